@@ -1,0 +1,358 @@
+#!/usr/bin/env python
+"""Throughput of the GB300 Siddon projector + backprojector.
+
+Workload (the differentiable-reconstruction configuration): float32 cube of
+256^3 voxels spanning [-1.5, 1.5] solar radii, 360 conic views of 512 x 512
+pixels over 0-360 deg at d = 215 solar radii, obstacle = "sun", seeded
+shell + blob phantom.  One step = one projection of the cube into the
+(zeroed) data stack + one backprojection of that stack into a (zeroed) cube,
+i.e. the operator work of one CG / gradient iteration, over all
+512 * 512 * 360 = 94,371,840 rays.
+
+metric "proj+backproj rays/s": rays per second through a projection +
+backprojection pair (value = N_gpus * rays / step time).  Multi-GPU runs are
+independent replicas (the path's only cross-view exchange is the sum of cube
+partials, which this single-GPU deployment does not need): scaling "weak".
+
+Lines printed (one JSON line from rank 0):
+  default          our kernels (CUDA events on the launching stream; L2 flushed
+                   between steps by a 256 MiB write), plus the e2e figure through
+                   the public operator API with pinned host buffers, the
+                   roofline of the dominant kernel and a CPU baseline;
+  --impl reference the reference algorithm's CPU implementation (the oracle's C
+                   restatement, float32, all host threads) on a bounded sample
+                   of the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "proj+backproj rays/s"
+UNIT = "rays/s"
+WORKLOAD = "cfg1"
+WORKLOAD_DESC = ("differentiable-reconstruction geometry: 256^3 f32 cube on [-1.5,1.5] Rsun, 360 views of "
+                 "512x512 over 0-360 deg at d=215 Rsun, obstacle=sun; step = projection + backprojection")
+L2_FLUSH_BYTES = 256 << 20
+CPU_SAMPLE_VIEWS = 16
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+
+class Clocks:
+    FIELDS = ("uuid,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, uuid=None):
+        self.uuid = uuid
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_%d.csv" % os.getpid())
+        self.proc = None
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            if self.uuid and self.uuid not in p[0] and p[0] not in self.uuid:
+                continue
+            rows.append(p)
+        if not rows:
+            return None
+        try:
+            sm = [float(r[1]) for r in rows]
+            smax = max(float(r[2]) for r in rows)
+            power = [float(r[3]) for r in rows]
+        except ValueError:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        pmax = max(power)
+        loaded = [s for s, pw in zip(sm, power) if pw >= 0.5 * pmax] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": smax, "reasons": reasons,
+                "samples": len(rows), "power_w_max": pmax}
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary (profiles/siddon_bpj_f32_cfg1.md), scaled to the full workload."""
+    path = os.path.join(ROOT, "profiles", "siddon_bpj_f32_cfg1.md")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch_full_workload:"):
+                return float(line.split(":")[1].split()[0])
+    except Exception:
+        pass
+    return None
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle (C restatement of the reference's OpenMP kernel)
+
+_CPU_CACHE = {}
+
+
+def cpu_sample(n_views=CPU_SAMPLE_VIEWS, threads=None, repeats=1):
+    import numpy as np
+
+    import oracle
+    from tomograpy_gb300 import synthetic
+    from tomograpy_gb300.infoarray import InfoArray
+    cfg = synthetic.CONFIGS[WORKLOAD]
+    if "geom" not in _CPU_CACHE:
+        ch, vh = synthetic.make_geometry(WORKLOAD)
+        _CPU_CACHE["geom"] = (ch, vh, synthetic.phantom(ch, seed=0))
+    ch, vh, x = _CPU_CACHE["geom"]
+    idx = np.linspace(0, cfg["T"] - 1, n_views).round().astype(int)
+    sub = [dict(vh[i]) for i in idx]
+    threads = threads or os.cpu_count()
+    best = None
+    for _ in range(repeats):
+        data = InfoArray(shape=(cfg["N"], cfg["N"], n_views), header=sub, dtype=np.float32)
+        cube = InfoArray(data=x, header=dict(ch))
+        t0 = time.perf_counter()
+        oracle.projector(data, cube, obstacle="sun", nthread=threads)
+        bcube = InfoArray(shape=x.shape, header=dict(ch), dtype=np.float32)
+        oracle.backprojector(data, bcube, obstacle="sun", nthread=threads)
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    rays = cfg["N"] * cfg["N"] * n_views
+    return rays / best, best, threads, rays
+
+
+def cpu_baseline_entry(value, threads, sample):
+    return {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count()
+    times = []
+    for _ in range(args.warmup):
+        cpu_sample(threads=threads)
+    rays = None
+    for _ in range(args.steps):
+        _, dt, threads, rays = cpu_sample(threads=threads)
+        times.append(dt)
+    ms = 1000.0 * statistics.mean(times)
+    value = rays / (ms / 1000.0)
+    sample = ("oracle float32 (C/OpenMP restatement of tomograpy/C_siddon.c.template), %d of 360 views "
+              "(%d rays) per step, projection + backprojection, %d threads" % (CPU_SAMPLE_VIEWS, rays, threads))
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "description": WORKLOAD_DESC, "sample_views": CPU_SAMPLE_VIEWS,
+                   "parallelism": "host threads (OpenMP over views)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# our path
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    import tomograpy_gb300 as tg
+    from tomograpy_gb300 import lo_wrapper, siddon, synthetic
+
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    # CPU baseline first (host threads only; no GPU context yet)
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        v, dt, threads, rays = cpu_sample(threads=os.cpu_count())
+        cpu = cpu_baseline_entry(v, threads, "oracle float32 (C/OpenMP restatement of the reference kernel), "
+                                             "%d of 360 views (%d rays), projection + backprojection, %.1f s"
+                                 % (CPU_SAMPLE_VIEWS, rays, dt))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    cfg = synthetic.CONFIGS[WORKLOAD]
+    n, T, N = cfg["n"], cfg["T"], cfg["N"]
+    ch, vh = synthetic.make_geometry(WORKLOAD)
+    x = torch.from_numpy(synthetic.phantom(ch, seed=0)).to(dev)
+    views = siddon.upload_views(vh, None, dev)
+    mh = siddon.pack_map_header(ch)
+    y = torch.zeros((T, N, N), device=dev).permute(1, 2, 0)  # view-major storage, (N1, N2, T) view
+    c = torch.zeros((n, n, n), device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, device=dev)
+    rays = N * N * T
+
+    # exact intersection count (outside the timed region)
+    counts = siddon.segment_counts(views, mh, (n, n, n), N, N, T, obstacle="sun")
+    inter = float(counts.sum(dtype=torch.float64))
+    hit = float((counts > 0).sum())
+    del counts
+
+    def step():
+        y.zero_()
+        e[0].record()
+        siddon.run_device("pj", y, x, views, mh, T, obstacle="sun")
+        e[1].record()
+        c.zero_()
+        e[2].record()
+        siddon.run_device("bpj", y, c, views, mh, T, obstacle="sun")
+        e[3].record()
+
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    for _ in range(args.warmup):
+        flush.fill_(1.0)
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    props = torch.cuda.get_device_properties(dev)
+    clocks = Clocks(str(getattr(props, "uuid", "")) or None)
+    clocks.start()
+    time.sleep(0.3)
+    pj_ms, bpj_ms, step_ms = [], [], []
+    s0 = torch.cuda.Event(enable_timing=True)
+    s1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    for _ in range(args.steps):
+        flush.fill_(1.0)  # L2 flush between steps (not timed)
+        s0.record()
+        step()
+        s1.record()
+        torch.cuda.synchronize()
+        pj_ms.append(e[0].elapsed_time(e[1]))
+        bpj_ms.append(e[2].elapsed_time(e[3]))
+        step_ms.append(s0.elapsed_time(s1))
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clk = clocks.stop()
+    ms = statistics.mean(step_ms)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * rays / (ms / 1000.0)
+
+    # roofline of the dominant kernel (algorithmic bytes per launch / its mean duration)
+    peak, peak_kind = measured_peak()
+    kern = {
+        "siddon_pj_f32": {"ms": statistics.mean(pj_ms), "bytes": 4.0 * inter + 4.0 * hit},
+        "siddon_bpj_f32": {"ms": statistics.mean(bpj_ms), "bytes": 8.0 * inter + 4.0 * hit},
+    }
+    for k in kern.values():
+        k["gbs"] = k["bytes"] / (k["ms"] / 1000.0) / 1e9
+        k["frac"] = k["gbs"] / peak
+    dom = max(kern, key=lambda k: kern[k]["ms"])
+    traffic = ncu_traffic() if dom == "siddon_bpj_f32" else None
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": kern[dom]["gbs"], "peak": peak, "unit": "GB/s",
+                "frac": kern[dom]["frac"], "traffic": traffic, "peak_kind": peak_kind + " hbm_gbs",
+                "algorithmic_bytes_per_launch": kern[dom]["bytes"]}
+
+    # end to end through the public operator API with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        op = lo_wrapper.siddon_lo(vh, ch, obstacle="sun", dtype=np.float32, device=dev)
+        xh = x.cpu().pin_memory()
+        yh = torch.empty((N, N, T), dtype=torch.float32).pin_memory()
+        chost = torch.empty((n, n, n), dtype=torch.float32).pin_memory()
+        for _ in range(max(1, args.warmup)):
+            op.project(xh, out=yh)
+            op.backproject(yh, out=chost)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            op.project(xh, out=yh)
+            op.backproject(yh, out=chost)
+        torch.cuda.synchronize()
+        e2e_ms = 1000.0 * (time.perf_counter() - t0) / args.steps
+        vol = n * n * n * 4
+        img = N * N * T * 4
+        e2e = {"value": world * rays / (e2e_ms / 1000.0), "unit": UNIT, "ms_per_step": e2e_ms,
+               "h2d_bytes_per_step": vol + img, "d2h_bytes_per_step": img + vol,
+               "path": "lo_wrapper.siddon_lo project/backproject, pinned host tensors"}
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "description": WORKLOAD_DESC, "rays_per_step": rays,
+                       "intersections_per_step": inter, "hit_rays_per_step": hit,
+                       "l2": "flushed between steps (256 MiB write, untimed)", "parallelism": "replicas"},
+            "intersections_per_s": world * inter * 2 / (ms / 1000.0),
+            "kernels": {k: {"ms": v["ms"], "GB_s": v["gbs"], "frac": v["frac"]} for k, v in kern.items()},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": 2 * args.steps,
+            "clocks": clk,
+        }
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,103 @@
+"""Shared helpers of the test-suite: golden fixtures, header rebuilding, error
+metrics and the degenerate-ray classification used by the parity tests.
+
+Tolerances (float32 GPU path against the float64 reference / oracle):
+
+* images: per-pixel max relative error <= 1e-5 over pixels whose reference
+  value is >= 1e-3 of the image maximum and whose ray is not degenerate, and
+  normwise error max|dy| / max|y| <= 1e-5 over all non-degenerate pixels;
+* backprojected cubes: per-voxel max relative error <= 1e-4 over voxels >= 1e-3
+  of the cube maximum, normwise <= 1e-4 (degenerate rays masked out of both
+  sides);
+* adjoint: |<Px, y> - <x, P^T y>| / |<Px, y>| <= 1e-5.
+
+A ray is *degenerate* when a component of its direction is non-zero but
+smaller than 1e-12: it runs within 1e-12 rad of a plane family, so which side
+of a voxel plane it is traced on depends on the last bits of the set-up
+arithmetic (in the reference too).
+"""
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden", "reference_siddon.npz")
+
+VIEW_KEYS = ["CRPIX1", "CRPIX2", "CDELT1", "CDELT2", "CRVAL1", "CRVAL2", "M1", "M2", "M3"] + \
+    ["R%d_%d" % (i, j) for i in (1, 2, 3) for j in (1, 2, 3)]
+CUBE_KEYS = ["CDELT1", "CDELT2", "CDELT3", "PSHAPE1", "PSHAPE2", "PSHAPE3",
+             "MMIN1", "MMIN2", "MMIN3", "MMAX1", "MMAX2", "MMAX3"]
+
+IMG_TOL = 1e-5
+CUBE_TOL = 1e-4
+ADJ_TOL = 1e-5
+
+_golden = None
+
+
+def golden():
+    global _golden
+    if _golden is None:
+        _golden = dict(np.load(GOLDEN))
+    return _golden
+
+
+def views_from_array(a, n1, n2):
+    hdrs = []
+    for row in a:
+        h = {k: float(v) for k, v in zip(VIEW_KEYS, row)}
+        h.update({"NAXIS": 2, "NAXIS1": n1, "NAXIS2": n2, "BITPIX": -64})
+        hdrs.append(h)
+    return hdrs
+
+
+def cube_from_array(a, shape):
+    h = {k: float(v) for k, v in zip(CUBE_KEYS, a)}
+    h.update({"NAXIS": len(shape), "BITPIX": -64})
+    for i, n in enumerate(shape):
+        h["NAXIS%d" % (i + 1)] = int(n)
+    return h
+
+
+def golden_case(prefix, n1, n2, cube_shape):
+    g = golden()
+    return views_from_array(g[prefix + "_views"], n1, n2), cube_from_array(g[prefix + "_cube_hdr"], cube_shape)
+
+
+def unit_vectors(views, n1, n2):
+    """float64 ray directions (N1, N2, T, 3), reference formula in NumPy."""
+    T = len(views)
+    u = np.empty((n1, n2, T, 3))
+    for t, h in enumerate(views):
+        R = np.array([[h["R%d_%d" % (a, b)] for b in (1, 2, 3)] for a in (1, 2, 3)])
+        g = (np.arange(n1) - h["CRPIX1"] + 1) * h["CDELT1"] + h["CRVAL1"]
+        lam = (np.arange(n2) - h["CRPIX2"] + 1) * h["CDELT2"] + h["CRVAL2"]
+        L, G = np.meshgrid(lam, g)
+        u2 = np.stack([np.cos(L) * np.cos(G), np.cos(L) * np.sin(G), np.sin(L)], axis=-1)
+        u[:, :, t, :] = u2 @ R.T
+    return u
+
+
+def degenerate_rays(views, n1, n2):
+    u = unit_vectors(views, n1, n2)
+    a = np.abs(u)
+    return np.any((a > 0) & (a < 1e-12), axis=-1)
+
+
+def image_errors(y, ref, exclude=None):
+    """(per-pixel max relative over significant pixels, normwise) errors."""
+    y = np.asarray(y, np.float64)
+    ref = np.asarray(ref, np.float64)
+    keep = np.ones(ref.shape, bool) if exclude is None else ~exclude
+    scale = np.abs(ref[keep]).max() if keep.any() else 0.0
+    if scale == 0:
+        return 0.0, float(np.abs(y[keep]).max()) if keep.any() else 0.0
+    d = np.abs(y - ref)
+    norm = d[keep].max() / scale
+    sig = keep & (np.abs(ref) >= 1e-3 * scale)
+    rel = (d[sig] / np.abs(ref[sig])).max() if sig.any() else 0.0
+    return float(rel), float(norm)
+
+
+def rel_dot(a, b):
+    return abs(a - b) / max(abs(a), abs(b), 1e-300)

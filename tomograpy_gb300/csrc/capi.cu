@@ -1,0 +1,289 @@
+// C ABI of libtomograpy_gb300.so (declared in include/tomograpy_gb300.h):
+// argument validation, launch geometry and dispatch to the kernels.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "tg_internal.cuh"
+
+namespace {
+
+thread_local char g_err[512] = "";
+
+tg_status fail(tg_status st, const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return st;
+}
+
+tg_status launch_status(cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return TG_OK;
+  return fail(TG_ELAUNCH, "%s: %s", what, cudaGetErrorString(e));
+}
+
+bool finite3(const double *v) { return isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]); }
+
+// Validate the shared arguments and fill the kernel geometry.
+tg_status make_geometry(tg::Geometry &G, const tg_map_header *mh, const tg_image_header *views, int32_t n_views,
+                        int64_t n1, int64_t n2, const int64_t ds[3], const int64_t map_shape[4],
+                        const int64_t ms[4], const void *mask, tg_dtype mask_dtype, const int64_t ks[3],
+                        bool four_d, bool *idx64) {
+  memset(&G, 0, sizeof(G));
+  if (!mh) return fail(TG_EINVAL, "map header is NULL");
+  if (!finite3(mh->cdelt) || !finite3(mh->pshape) || !finite3(mh->mmin) || !finite3(mh->mmax))
+    return fail(TG_EINVAL, "map header has a non-finite value");
+  for (int k = 0; k < 3; ++k)
+    if (!(mh->cdelt[k] > 0.0) || !(mh->pshape[k] > 0.0))
+      return fail(TG_EINVAL, "map header CDELT%d / PSHAPE%d must be positive", k + 1, k + 1);
+  if (n_views < 0) return fail(TG_EINVAL, "negative number of views");
+  if (n_views > 0 && !views) return fail(TG_EINVAL, "view header table is NULL");
+  if (n1 < 0 || n2 < 0 || n1 > (1 << 24) || n2 > (1 << 24))
+    return fail(TG_EINVAL, "image shape (%lld, %lld) out of range", (long long)n1, (long long)n2);
+  if (!ds || !map_shape || !ms) return fail(TG_EINVAL, "stride / shape array is NULL");
+  for (int k = 0; k < 3; ++k)
+    if (map_shape[k] < 1 || map_shape[k] > (1 << 20))
+      return fail(TG_EINVAL, "cube axis %d has %lld voxels", k, (long long)map_shape[k]);
+  if (four_d && map_shape[3] < 1) return fail(TG_EINVAL, "4-D cube needs at least one frame");
+  if (mask) {
+    if (!ks) return fail(TG_EINVAL, "mask strides are NULL");
+    if (mask_dtype != TG_U8 && mask_dtype != TG_F32 && mask_dtype != TG_F64)
+      return fail(TG_EINVAL, "mask dtype must be u8, f32 or f64");
+  }
+  G.views = views;
+  G.n_views = n_views;
+  G.n1 = (int)n1;
+  G.n2 = (int)n2;
+  G.ray_i = G.ray_j = -1;
+  for (int k = 0; k < 3; ++k) {
+    G.ds[k] = ds[k];
+    G.ks[k] = mask ? ks[k] : 0;
+    G.n[k] = (int)map_shape[k];
+    G.ms[k] = ms[k];
+    G.mh.cdelt[k] = mh->cdelt[k];
+    G.mh.pshape[k] = mh->pshape[k];
+    G.mh.mmin[k] = mh->mmin[k];
+    G.mh.mmax[k] = mh->mmax[k];
+    G.cdeltf[k] = (float)mh->cdelt[k];
+    G.mminf[k] = (float)mh->mmin[k];
+    G.mmaxf[k] = (float)mh->mmax[k];
+    G.inv_cdelt[k] = 1.0 / mh->cdelt[k];
+  }
+  G.ms[3] = four_d ? ms[3] : 0;
+  G.nframes = four_d ? (int)map_shape[3] : 1;
+  G.mask = mask;
+  G.mask_dtype = (int)mask_dtype;
+  double span = 0.0;
+  for (int k = 0; k < 3; ++k) span += (double)(map_shape[k] - 1) * fabs((double)ms[k]);
+  *idx64 = span >= 2147483647.0;
+  return TG_OK;
+}
+
+tg_status project_views(const tg_map_header *mh, const tg_image_header *views, int32_t n_views, int32_t view0,
+                        int32_t count, int ray_i, int ray_j, tg_dtype dtype, void *data, int64_t n1, int64_t n2,
+                        const int64_t ds[3], void *map, const int64_t map_shape[4], const int64_t ms[4],
+                        const void *mask, tg_dtype mask_dtype, const int64_t ks[3], int32_t obstacle,
+                        int32_t mode, void *stream) {
+  if (mode < TG_PJ || mode > TG_BPJT) return fail(TG_EINVAL, "mode must be pj, bpj, pjt or bpjt");
+  if (obstacle != TG_OBSTACLE_NONE && obstacle != TG_OBSTACLE_SUN)
+    return fail(TG_EINVAL, "obstacle must be none or sun");
+  if (dtype != TG_F32 && dtype != TG_F64) return fail(TG_EINVAL, "data dtype must be f32 or f64");
+  if (!data || !map) return fail(TG_EINVAL, "data or map pointer is NULL");
+  const bool four_d = (mode == TG_PJT || mode == TG_BPJT);
+  tg::Geometry G;
+  bool idx64 = false;
+  tg_status st = make_geometry(G, mh, views, n_views, n1, n2, ds, map_shape, ms, mask, mask_dtype, ks, four_d,
+                               &idx64);
+  if (st != TG_OK) return st;
+  if (count <= 0 || n1 == 0 || n2 == 0) return TG_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  int gx, gy;
+  if (ray_i >= 0) {
+    G.ray_i = ray_i;
+    G.ray_j = ray_j;
+    G.mask_eq1 = 1;
+    G.bx0 = ray_j / 32;
+    G.by0 = ray_i / tg::kRows;
+    gx = gy = 1;
+  } else {
+    gx = (int)((n2 + 31) / 32);
+    gy = (int)((n1 + tg::kRows - 1) / tg::kRows);
+    if (gy > 65535) return fail(TG_EUNSUPPORTED, "image has too many rows (%lld)", (long long)n1);
+  }
+  for (int32_t v = 0; v < count; v += 65535) {
+    const int gz = (count - v) < 65535 ? (count - v) : 65535;
+    G.view0 = view0 + v;
+    cudaError_t e;
+    if (dtype == TG_F32)
+      e = tg::launch_fast_f32(G, mode, obstacle, idx64, (float *)data, (float *)map, gx, gy, gz, s);
+    else
+      e = tg::launch_ref_f64(G, mode, obstacle, (double *)data, (double *)map, gx, gy, gz, s);
+    if (e != cudaSuccess) return launch_status(e, "projector launch");
+  }
+  return TG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+tg_status tg_conic_full_projector(const tg_map_header *map_header, const tg_image_header *views, int32_t n_views,
+                                  tg_dtype dtype, void *data, int64_t n1, int64_t n2, const int64_t data_strides[3],
+                                  void *map, const int64_t map_shape[4], const int64_t map_strides[4],
+                                  const void *mask, tg_dtype mask_dtype, const int64_t mask_strides[3],
+                                  int32_t obstacle, int32_t mode, void *stream) {
+  return project_views(map_header, views, n_views, 0, n_views, -1, -1, dtype, data, n1, n2, data_strides, map,
+                       map_shape, map_strides, mask, mask_dtype, mask_strides, obstacle, mode, stream);
+}
+
+tg_status tg_conic_image_projector(const tg_map_header *map_header, const tg_image_header *views, int32_t n_views,
+                                   int32_t t, tg_dtype dtype, void *data, int64_t n1, int64_t n2,
+                                   const int64_t data_strides[3], void *map, const int64_t map_shape[4],
+                                   const int64_t map_strides[4], const void *mask, tg_dtype mask_dtype,
+                                   const int64_t mask_strides[3], int32_t obstacle, int32_t mode, void *stream) {
+  if (t < 0 || t >= n_views) return fail(TG_EINVAL, "view index %d outside [0, %d)", t, n_views);
+  return project_views(map_header, views, n_views, t, 1, -1, -1, dtype, data, n1, n2, data_strides, map,
+                       map_shape, map_strides, mask, mask_dtype, mask_strides, obstacle, mode, stream);
+}
+
+tg_status tg_ray_projector(const tg_map_header *map_header, const tg_image_header *views, int32_t n_views,
+                           int32_t i, int32_t j, int32_t t, tg_dtype dtype, void *data, int64_t n1, int64_t n2,
+                           const int64_t data_strides[3], void *map, const int64_t map_shape[4],
+                           const int64_t map_strides[4], const void *mask, tg_dtype mask_dtype,
+                           const int64_t mask_strides[3], int32_t obstacle, int32_t mode, void *stream) {
+  if (t < 0 || t >= n_views) return fail(TG_EINVAL, "view index %d outside [0, %d)", t, n_views);
+  if (i < 0 || i >= n1 || j < 0 || j >= n2) return fail(TG_EINVAL, "pixel (%d, %d) outside the image", i, j);
+  return project_views(map_header, views, n_views, t, 1, i, j, dtype, data, n1, n2, data_strides, map, map_shape,
+                       map_strides, mask, mask_dtype, mask_strides, obstacle, mode, stream);
+}
+
+tg_status tg_unit_vector(const tg_image_header *views, int32_t n_views, int32_t t, tg_dtype dtype,
+                         const void *data, int64_t n1, int64_t n2, const int64_t data_strides[3], double *u,
+                         const int64_t u_strides[4], void *stream) {
+  if (dtype != TG_F32 && dtype != TG_F64) return fail(TG_EINVAL, "data dtype must be f32 or f64");
+  if (!views || !data || !u || !data_strides || !u_strides) return fail(TG_EINVAL, "NULL argument");
+  if (n1 < 0 || n2 < 0 || n1 > 65535 || n2 > (1 << 24)) return fail(TG_EINVAL, "image shape out of range");
+  if (t < -1 || t >= n_views) return fail(TG_EINVAL, "view index %d outside [-1, %d)", t, n_views);
+  if (n1 == 0 || n2 == 0 || n_views == 0) return TG_OK;
+  tg::Geometry G;
+  memset(&G, 0, sizeof(G));
+  G.views = views;
+  G.n_views = n_views;
+  G.n1 = (int)n1;
+  G.n2 = (int)n2;
+  for (int k = 0; k < 3; ++k) G.ds[k] = data_strides[k];
+  const long long us[4] = {u_strides[0], u_strides[1], u_strides[2], u_strides[3]};
+  const int count = (t < 0) ? n_views : 1;
+  for (int v = 0; v < count; v += 65535) {
+    G.view0 = (t < 0 ? 0 : t) + v;
+    const int gz = (count - v) < 65535 ? (count - v) : 65535;
+    cudaError_t e = tg::launch_unit_vector(G, dtype == TG_F64, data, u, us, (int)((n2 + 127) / 128), (int)n1, gz,
+                                           (cudaStream_t)stream);
+    if (e != cudaSuccess) return launch_status(e, "unit vector launch");
+  }
+  return TG_OK;
+}
+
+tg_status tg_intersection_parameters(const tg_map_header *map_header, const tg_image_header *views,
+                                     int32_t n_views, int32_t t, tg_dtype dtype, int64_t n1, int64_t n2,
+                                     const double *u, const int64_t u_strides[4], double *a1, double *an,
+                                     void *stream) {
+  if (dtype != TG_F32 && dtype != TG_F64) return fail(TG_EINVAL, "dtype must be f32 or f64");
+  if (!map_header || !views || !u || !u_strides || !a1 || !an) return fail(TG_EINVAL, "NULL argument");
+  if (n1 < 0 || n2 < 0 || n1 > 65535 || n2 > (1 << 24)) return fail(TG_EINVAL, "image shape out of range");
+  if (t < -1 || t >= n_views) return fail(TG_EINVAL, "view index %d outside [-1, %d)", t, n_views);
+  if (n1 == 0 || n2 == 0 || n_views == 0) return TG_OK;
+  tg::Geometry G;
+  memset(&G, 0, sizeof(G));
+  G.views = views;
+  G.n_views = n_views;
+  G.n1 = (int)n1;
+  G.n2 = (int)n2;
+  G.mh = *map_header;
+  const long long us[4] = {u_strides[0], u_strides[1], u_strides[2], u_strides[3]};
+  const int count = (t < 0) ? n_views : 1;
+  for (int v = 0; v < count; v += 65535) {
+    G.view0 = (t < 0 ? 0 : t) + v;
+    const int gz = (count - v) < 65535 ? (count - v) : 65535;
+    cudaError_t e = tg::launch_intersection_parameters(G, dtype == TG_F64, u, us, a1, an, (int)((n2 + 127) / 128),
+                                                       (int)n1, gz, (cudaStream_t)stream);
+    if (e != cudaSuccess) return launch_status(e, "intersection parameters launch");
+  }
+  return TG_OK;
+}
+
+size_t tg_deterministic_workspace_bytes(const int64_t map_shape[4]) {
+  if (!map_shape) return 0;
+  size_t vox = 1;
+  for (int k = 0; k < 4; ++k) vox *= (size_t)(map_shape[k] > 0 ? map_shape[k] : 1);
+  size_t bytes = 256 + vox * 8;
+  return (bytes + 255) & ~(size_t)255;
+}
+
+tg_status tg_conic_full_backprojector_deterministic(
+    const tg_map_header *map_header, const tg_image_header *views, int32_t n_views, float *data, int64_t n1,
+    int64_t n2, const int64_t data_strides[3], float *map, const int64_t map_shape[4], const int64_t map_strides[4],
+    const void *mask, tg_dtype mask_dtype, const int64_t mask_strides[3], int32_t obstacle, int32_t mode,
+    void *workspace, size_t workspace_bytes, void *stream) {
+  if (mode != TG_BPJ && mode != TG_BPJT) return fail(TG_EINVAL, "deterministic mode is for bpj / bpjt");
+  if (obstacle != TG_OBSTACLE_NONE && obstacle != TG_OBSTACLE_SUN)
+    return fail(TG_EINVAL, "obstacle must be none or sun");
+  if (!data || !map) return fail(TG_EINVAL, "data or map pointer is NULL");
+  if (!workspace || ((uintptr_t)workspace & 255u)) return fail(TG_EINVAL, "workspace must be 256-byte aligned");
+  const bool four_d = (mode == TG_BPJT);
+  int64_t shape4[4] = {map_shape ? map_shape[0] : 0, map_shape ? map_shape[1] : 0, map_shape ? map_shape[2] : 0,
+                       four_d && map_shape ? map_shape[3] : 1};
+  if (workspace_bytes < tg_deterministic_workspace_bytes(shape4))
+    return fail(TG_ENOMEM, "workspace has %zu bytes, needs %zu", workspace_bytes,
+                tg_deterministic_workspace_bytes(shape4));
+  tg::Geometry G;
+  bool idx64 = false;
+  tg_status st = make_geometry(G, map_header, views, n_views, n1, n2, data_strides, map_shape, map_strides, mask,
+                               mask_dtype, mask_strides, four_d, &idx64);
+  if (st != TG_OK) return st;
+  if (n_views == 0 || n1 == 0 || n2 == 0) return TG_OK;
+  // accumulator offsets are dense C order (n0, n1, n2) within a frame
+  const double span = (double)G.n[0] * G.n[1] * G.n[2];
+  idx64 = span >= 2147483647.0;
+  const int gx = (int)((n2 + 31) / 32), gy = (int)((n1 + tg::kRows - 1) / tg::kRows);
+  if (gy > 65535) return fail(TG_EUNSUPPORTED, "image has too many rows");
+  if (n_views > 65535) return fail(TG_EUNSUPPORTED, "deterministic mode takes at most 65535 views per call");
+  G.view0 = 0;
+  cudaError_t e = tg::launch_deterministic_bpj(G, mode, obstacle, idx64, data, map, workspace, gx, gy, n_views,
+                                               (cudaStream_t)stream);
+  return launch_status(e, "deterministic backprojection launch");
+}
+
+tg_status tg_segment_counts(const tg_map_header *map_header, const tg_image_header *views, int32_t n_views,
+                            float *counts, int64_t n1, int64_t n2, const int64_t count_strides[3],
+                            const int64_t map_shape[3], const void *mask, tg_dtype mask_dtype,
+                            const int64_t mask_strides[3], int32_t obstacle, void *stream) {
+  if (obstacle != TG_OBSTACLE_NONE && obstacle != TG_OBSTACLE_SUN)
+    return fail(TG_EINVAL, "obstacle must be none or sun");
+  if (!counts || !map_shape) return fail(TG_EINVAL, "NULL argument");
+  const int64_t shape4[4] = {map_shape[0], map_shape[1], map_shape[2], 1};
+  const int64_t strides4[4] = {map_shape[1] * map_shape[2], map_shape[2], 1, 0};
+  tg::Geometry G;
+  bool idx64 = false;
+  tg_status st = make_geometry(G, map_header, views, n_views, n1, n2, count_strides, shape4, strides4, mask,
+                               mask_dtype, mask_strides, false, &idx64);
+  if (st != TG_OK) return st;
+  if (n_views == 0 || n1 == 0 || n2 == 0) return TG_OK;
+  const int gx = (int)((n2 + 31) / 32), gy = (int)((n1 + tg::kRows - 1) / tg::kRows);
+  if (gy > 65535) return fail(TG_EUNSUPPORTED, "image has too many rows");
+  for (int32_t v = 0; v < n_views; v += 65535) {
+    G.view0 = v;
+    const int gz = (n_views - v) < 65535 ? (n_views - v) : 65535;
+    cudaError_t e = tg::launch_count_f32(G, obstacle, idx64, counts, gx, gy, gz, (cudaStream_t)stream);
+    if (e != cudaSuccess) return launch_status(e, "segment count launch");
+  }
+  return TG_OK;
+}
+
+const char *tg_last_error(void) { return g_err; }
+
+int32_t tg_abi_version(void) { return 1; }
+
+}  // extern "C"

@@ -1,0 +1,75 @@
+// Internal declarations shared by the CUDA translation units of
+// libtomograpy_gb300.so.  Not part of the public ABI (include/tomograpy_gb300.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/tomograpy_gb300.h"
+
+namespace tg {
+
+// Rows of pixels (one warp each) per CTA; a warp covers 32 consecutive pixels
+// of one row (image axis 1, the lambda axis), so that for equatorial observers
+// its 32 rays walk neighbouring voxels of the cube's fastest axis.
+constexpr int kRows = 8;
+constexpr int kThreads = 32 * kRows;
+
+// The reference's finite "infinity" for zero direction components
+// (tomograpy/C_siddon.c.template:17).
+constexpr double kRefInf = 100000.0;
+
+// Direction components below this magnitude are treated as exactly zero by
+// the fast f32 kernel (a ray lying within 1e-14 rad of a voxel-plane family is
+// traced as lying in it).  The f64 kernel keeps the reference's behaviour.
+constexpr double kSnapZero = 1e-14;
+
+// Launch description shared by all projector kernels.
+struct Geometry {
+  const tg_image_header *views;
+  int n_views;
+  int view0;           // first view of this launch (grid.z offset)
+  int n1, n2;          // image rows (axis 0, gamma) / columns (axis 1, lambda)
+  int bx0, by0;        // tile offsets (single-ray launches)
+  int ray_i, ray_j;    // >= 0: trace only this pixel
+  long long ds[3];     // data strides (elements)
+  const void *mask;
+  long long ks[3];
+  int mask_dtype;      // tg_dtype
+  int mask_eq1;        // 1: skip when mask == 1 (ray_projector); 0: skip when mask != 0
+  int n[3];            // cube voxels per axis
+  int nframes;         // frames of a 4-D cube (1 for 3-D)
+  long long ms[4];     // cube strides (elements)
+  tg_map_header mh;
+  float cdeltf[3], mminf[3], mmaxf[3];
+  double inv_cdelt[3];
+};
+
+// Read the mask of pixel (i, j, t); true when the ray must be skipped.
+__device__ __forceinline__ bool masked(const Geometry &G, int i, int j, int t) {
+  if (G.mask == nullptr) return false;
+  long long o = (long long)i * G.ks[0] + (long long)j * G.ks[1] + (long long)t * G.ks[2];
+  double v;
+  if (G.mask_dtype == TG_U8) v = (double)((const unsigned char *)G.mask)[o];
+  else if (G.mask_dtype == TG_F32) v = (double)((const float *)G.mask)[o];
+  else v = ((const double *)G.mask)[o];
+  return G.mask_eq1 ? (v == 1.0) : (v != 0.0);
+}
+
+// Host-side launchers (return a cudaError_t of the launch).
+cudaError_t launch_fast_f32(const Geometry &G, int mode, int obstacle, bool idx64, float *data, float *map,
+                            int grid_x, int grid_y, int grid_z, cudaStream_t s);
+cudaError_t launch_count_f32(const Geometry &G, int obstacle, bool idx64, float *counts, int grid_x, int grid_y,
+                             int grid_z, cudaStream_t s);
+cudaError_t launch_ref_f64(const Geometry &G, int mode, int obstacle, double *data, double *map, int grid_x,
+                           int grid_y, int grid_z, cudaStream_t s);
+cudaError_t launch_unit_vector(const Geometry &G, int ctype_f64, const void *data, double *u,
+                               const long long us[4], int grid_x, int grid_y, int grid_z, cudaStream_t s);
+cudaError_t launch_intersection_parameters(const Geometry &G, int ctype_f64, const double *u,
+                                           const long long us[4], double *a1, double *an, int grid_x,
+                                           int grid_y, int grid_z, cudaStream_t s);
+cudaError_t launch_deterministic_bpj(const Geometry &G, int mode, int obstacle, bool idx64, const float *data,
+                                     float *map, void *workspace, int grid_x, int grid_y, int grid_z,
+                                     cudaStream_t s);
+
+}  // namespace tg

@@ -1,0 +1,159 @@
+"""Linear-operator wrappers of the projector: ``siddon_lo`` / ``siddon4d_lo``.
+
+TomograPy wraps its projector for the ``lo`` package (``tomograpy/lo_wrapper.py:10-73``):
+``matvec`` = zero the output, project; ``rmatvec`` = zero the output,
+backproject; the 4-D operator loops over ``ng`` interleaved sub-stacks, view
+``j`` of sub-stack ``i`` (global view ``i + j*ng``) reading cube frame ``j``.
+``lo`` is not available here, so :class:`Siddon` is a
+``scipy.sparse.linalg.LinearOperator`` with the same behaviour on flattened
+NumPy vectors, plus a device-resident interface (:meth:`Siddon.project`,
+:meth:`Siddon.backproject`) on torch tensors that CG loops use without any
+host round trip.
+
+Differences from the reference, on purpose:
+
+* the geometry (view table, cube header) is uploaded to the GPU once, at
+  construction, instead of being re-marshalled at every call;
+* ``matvec`` / ``rmatvec`` return a fresh array (the reference returns the
+  same buffer at every call, ``tomograpy/lo_wrapper.py:25,31``, so its callers
+  must copy);
+* the 4-D operator maps every view to its frame in one launch (frame =
+  view // ng) instead of ``ng`` launches over strided sub-stacks, and its
+  ``rmatvec`` uses the data headers of the sub-stack (the reference assigns
+  ``xi.header = xi.header[i::ng]``, ``tomograpy/lo_wrapper.py:63``).
+"""
+import numpy as np
+
+from . import siddon as S
+
+try:
+    import torch
+except ImportError:  # pragma: no cover
+    torch = None
+
+from scipy.sparse.linalg import LinearOperator
+
+
+class Siddon(LinearOperator):
+    """Projector ``P`` (cube -> data) as a linear operator.
+
+    Parameters mirror ``tomograpy.lo_wrapper.Siddon(data_header, cube_header,
+    **kwargs)``; ``kwargs`` may hold ``mask`` and ``obstacle`` as for
+    ``projector``.  ``frames`` (4-D only) gives the cube frame of each view.
+    """
+
+    def __init__(self, data_header, cube_header, mask=None, obstacle=None, dtype=np.float32, frames=None,
+                 cube_shape=None, deterministic=False, device=None, nthread=0):
+        self.data_header = [dict(h) for h in data_header]
+        self.map_header = dict(cube_header)
+        if "MMAX1" not in self.map_header:
+            S.H.map_borders(self.map_header)
+        for h in self.data_header:
+            if "R1_1" not in h:
+                S.H.header_rotation_matrix(h)
+        h0 = self.data_header[0]
+        self.n1, self.n2, self.T = int(h0["NAXIS1"]), int(h0["NAXIS2"]), len(self.data_header)
+        if cube_shape is None:
+            cube_shape = tuple(int(self.map_header["NAXIS%d" % (k + 1)]) for k in range(3))
+        self.cube_shape = tuple(int(v) for v in cube_shape)
+        self.four_d = len(self.cube_shape) == 4
+        self.frames = None
+        if self.four_d:
+            fr = np.arange(self.T) if frames is None else np.asarray(frames)
+            if fr.min() < 0 or fr.max() >= self.cube_shape[3]:
+                raise ValueError("view frame index outside the cube's frames")
+            self.frames = fr
+        self.device = device or S._device()
+        self.tdtype = torch.float32 if np.dtype(dtype) == np.float32 else torch.float64
+        self.views_dev = S.upload_views(self.data_header, self.frames, self.device)
+        self.mh = S.pack_map_header(self.map_header)
+        self.mask = S._mask_to_device(mask, self.device) if mask is not None else None
+        self.obstacle = obstacle
+        self.deterministic = deterministic
+        self._workspace = None
+        self.data_shape = (self.n1, self.n2, self.T)
+        n_in = int(np.prod(self.cube_shape))
+        n_out = int(np.prod(self.data_shape))
+        super().__init__(dtype=np.dtype(dtype), shape=(n_out, n_in))
+
+    # -- device interface ------------------------------------------------
+    def _dev(self, a, shape):
+        if torch.is_tensor(a):
+            t = a if a.is_cuda else a.to(self.device, non_blocking=True)
+        else:
+            t = torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=self.dtype))).to(self.device)
+        return t.reshape(shape)
+
+    def project(self, x, out=None):
+        """y = P x.  ``x``: cube (CUDA or host tensor / array).  Returns a CUDA
+        tensor, or fills ``out`` (device or host tensor) and returns it."""
+        xd = self._dev(x, self.cube_shape)
+        y = torch.zeros(self.data_shape, dtype=self.tdtype, device=self.device)
+        S.run_device("pjt" if self.four_d else "pj", y, xd, self.views_dev, self.mh, self.T, self.mask,
+                     self.obstacle)
+        return self._out(y, out)
+
+    def backproject(self, y, out=None):
+        """x = P^T y.  ``y``: data stack (CUDA or host tensor / array)."""
+        yd = self._dev(y, self.data_shape)
+        x = torch.zeros(self.cube_shape, dtype=self.tdtype, device=self.device)
+        if self.deterministic and self.tdtype == torch.float32:
+            from . import _lib
+            need = _lib.load().tg_deterministic_workspace_bytes(
+                _lib.i64(list(self.cube_shape) + ([] if self.four_d else [1])))
+            if self._workspace is None or self._workspace.numel() < need:
+                self._workspace = torch.empty(need, dtype=torch.uint8, device=self.device)
+            S.run_device("bpjt" if self.four_d else "bpj", yd, x, self.views_dev, self.mh, self.T, self.mask,
+                         self.obstacle, deterministic=True, workspace=self._workspace)
+        else:
+            S.run_device("bpjt" if self.four_d else "bpj", yd, x, self.views_dev, self.mh, self.T, self.mask,
+                         self.obstacle)
+        return self._out(x, out)
+
+    def _out(self, r, out):
+        if out is None:
+            return r
+        out.view(r.shape).copy_(r, non_blocking=True)
+        if not out.is_cuda:
+            torch.cuda.current_stream().synchronize()
+        return out
+
+    # -- scipy LinearOperator interface (flattened NumPy vectors) ----------
+    def _matvec(self, x):
+        return self.project(np.asarray(x).reshape(self.cube_shape)).reshape(-1).cpu().numpy()
+
+    def _rmatvec(self, y):
+        return self.backproject(np.asarray(y).reshape(self.data_shape)).reshape(-1).cpu().numpy()
+
+    def _adjoint(self):
+        return _Adjoint(self)
+
+
+class _Adjoint(LinearOperator):
+    def __init__(self, op):
+        self.op = op
+        super().__init__(dtype=op.dtype, shape=(op.shape[1], op.shape[0]))
+
+    def _matvec(self, y):
+        return self.op._rmatvec(y)
+
+    def _rmatvec(self, x):
+        return self.op._matvec(x)
+
+
+def siddon_lo(data_header, cube_header, **kwargs):
+    """3-D projector operator (tomograpy/lo_wrapper.py:69-70)."""
+    return Siddon(data_header, cube_header, **kwargs)
+
+
+def siddon4d_lo(data_header, cube_header, ng=1, **kwargs):
+    """4-D projector operator: the stack is split into ``ng`` interleaved
+    sub-stacks and view ``i + j*ng`` uses cube frame ``j``
+    (tomograpy/lo_wrapper.py:38-67,72-73)."""
+    T = len(data_header)
+    frames = np.arange(T) // int(ng)
+    ch = dict(cube_header)
+    cube_shape = kwargs.pop("cube_shape", None)
+    if cube_shape is None:
+        cube_shape = tuple(int(ch["NAXIS%d" % (k + 1)]) for k in range(3)) + (int(frames.max()) + 1,)
+    return Siddon(data_header, cube_header, frames=frames, cube_shape=cube_shape, **kwargs)

@@ -156,6 +156,14 @@ tg_status tg_segment_counts(const tg_map_header *map_header, const tg_image_head
                             const int64_t map_shape[3], const void *mask, tg_dtype mask_dtype,
                             const int64_t mask_strides[3], int32_t obstacle, void *stream);
 
+/* out[0] = sum_i a[i] * b[i] over n float32 elements, accumulated in float64
+ * with a fixed reduction order (bitwise reproducible).  The inner product of
+ * the CG driver (TomograPy delegates CG to the external lo package,
+ * tomograpy/srt.py:225); workspace of tg_dot_workspace_bytes() bytes. */
+size_t tg_dot_workspace_bytes(void);
+tg_status tg_dot_f32(const float *a, const float *b, int64_t n, double *out, void *workspace,
+                     size_t workspace_bytes, void *stream);
+
 /* Message for the last non-OK status returned on this thread. */
 const char *tg_last_error(void);
 

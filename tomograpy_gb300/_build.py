@@ -22,6 +22,7 @@ UNITS = {
     "siddon_fast.cu": [],
     "siddon_ref.cu": ["--fmad=false"],
     "deterministic.cu": [],
+    "reduce.cu": [],
     "capi.cu": [],
 }
 

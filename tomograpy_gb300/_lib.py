@@ -61,7 +61,10 @@ def load(build_if_missing=True):
     L.tg_conic_full_backprojector_deterministic.argtypes = proj_args[:3] + [P, I64, I64, P, P, P, P, P, I32, P,
                                                                             I32, I32, P, SZ, P]
     L.tg_segment_counts.argtypes = [P, P, I32, P, I64, I64, P, P, P, I32, P, I32, P]
-    for name in ("tg_segment_counts", "tg_conic_full_projector", "tg_conic_image_projector", "tg_ray_projector", "tg_unit_vector",
+    L.tg_dot_workspace_bytes.argtypes = []
+    L.tg_dot_workspace_bytes.restype = SZ
+    L.tg_dot_f32.argtypes = [P, P, I64, P, P, SZ, P]
+    for name in ("tg_dot_f32", "tg_segment_counts", "tg_conic_full_projector", "tg_conic_image_projector", "tg_ray_projector", "tg_unit_vector",
                  "tg_intersection_parameters", "tg_conic_full_backprojector_deterministic"):
         getattr(L, name).restype = ctypes.c_int
     L.tg_last_error.restype = ctypes.c_char_p

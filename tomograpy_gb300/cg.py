@@ -1,0 +1,142 @@
+"""Conjugate gradients on the GPU around the projector.
+
+TomograPy solves its models with ``lo.acg`` (``tomograpy/srt.py:225``,
+``tests/test_models.py:31``): CG on the regularised normal equations
+(P^T P + sum_i h_i D_i^T D_i) x = P^T y, written out at
+``exemples/test_siddon_cgs_secchi.py:32-33``, with D_i the finite differences
+of ``lo.diff`` along each cube axis (``tomograpy/models.py:85-94``).  ``lo`` is
+a third-party package absent from the reference tree; this module restates
+textbook CG (Hestenes-Stiefel) for that system:
+
+* vectors in float32 on the device; inner products and residual norms
+  accumulated in float64 (``tg_dot_f32``, a fixed-order reduction);
+* scalars (alpha, beta, residual norms) stay on the device as 0-d tensors, so
+  an iteration needs no host synchronisation and can be captured once in a
+  CUDA graph and replayed (``graph=True``).
+"""
+import ctypes
+
+import torch
+
+from . import _lib
+
+
+class Dot:
+    """float64-accumulated inner products of float32 device vectors."""
+
+    def __init__(self, device, n_slots=8):
+        L = _lib.load()
+        self.ws = torch.empty(L.tg_dot_workspace_bytes() // 8, dtype=torch.float64, device=device)
+        self.out = torch.zeros(n_slots, dtype=torch.float64, device=device)
+
+    def __call__(self, a, b, slot=0):
+        L = _lib.load()
+        a = a.reshape(-1)
+        b = b.reshape(-1)
+        if a.dtype != torch.float32 or b.dtype != torch.float32 or not (a.is_contiguous() and b.is_contiguous()):
+            raise ValueError("dot takes contiguous float32 vectors")
+        st = L.tg_dot_f32(ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(b.data_ptr()), a.numel(),
+                          ctypes.c_void_p(self.out.data_ptr() + 8 * slot), ctypes.c_void_p(self.ws.data_ptr()),
+                          self.ws.numel() * 8, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        _lib.check(st)
+        return self.out[slot]
+
+
+def diff_normal(x, axis):
+    """D^T D x for the forward difference D along ``axis`` (lo.diff's operator)."""
+    d = torch.diff(x, dim=axis)
+    out = torch.zeros_like(x)
+    n = x.shape[axis]
+    out.narrow(axis, 0, n - 1).sub_(d)
+    out.narrow(axis, 1, n - 1).add_(d)
+    return out
+
+
+class NormalOperator:
+    """A x = P^T P x + lam x + sum_i h_i D_i^T D_i x (+ mu D_t^T D_t x for 4-D).
+
+    ``P`` is a :class:`tomograpy_gb300.lo_wrapper.Siddon`; ``hypers`` are the
+    h_i of the spatial finite-difference priors (axes 0..2), ``temporal`` the
+    weight of the frame-difference prior of a 4-D cube (axis 3).
+    """
+
+    def __init__(self, P, lam=0.0, hypers=(), temporal=0.0):
+        self.P = P
+        self.lam = float(lam)
+        self.hypers = tuple(float(h) for h in hypers)
+        self.temporal = float(temporal)
+
+    def __call__(self, x):
+        y = self.P.project(x)
+        out = self.P.backproject(y)
+        if self.lam:
+            out.add_(x, alpha=self.lam)
+        for axis, h in enumerate(self.hypers):
+            if h:
+                out.add_(diff_normal(x, axis), alpha=h)
+        if self.temporal and x.dim() == 4 and x.shape[3] > 1:
+            out.add_(diff_normal(x, 3), alpha=self.temporal)
+        return out
+
+
+class CGResult:
+    def __init__(self, x, iterations, residuals):
+        self.x = x
+        self.iterations = iterations
+        self.residuals = residuals  # ||r_k|| / ||b||, float64 host list
+
+
+def cg(A, b, x0=None, maxiter=10, tol=0.0, graph=False):
+    """Solve A x = b (A symmetric positive definite, callable on device tensors).
+
+    Runs ``maxiter`` iterations (stopping early on the host only when
+    ``tol`` > 0 and ``graph`` is False).  Returns a :class:`CGResult`.
+    """
+    dev = b.device
+    dot = Dot(dev, n_slots=4)
+    x = torch.zeros_like(b) if x0 is None else x0.clone()
+    r = b - A(x) if x0 is not None else b.clone()
+    p = r.clone()
+    rr = dot(r, r, 0).clone()
+    bb = dot(b, b, 1).clone()
+    hist = torch.zeros(maxiter + 1, dtype=torch.float64, device=dev)
+    hist[0] = torch.sqrt(rr / bb)
+    k_dev = torch.zeros((), dtype=torch.int64, device=dev)
+
+    def step():
+        Ap = A(p)
+        pAp = dot(p, Ap, 2)
+        alpha = rr / pAp
+        x.add_(p * alpha.to(torch.float32))
+        r.sub_(Ap * alpha.to(torch.float32))
+        rr_new = dot(r, r, 3)
+        beta = rr_new / rr
+        p.mul_(beta.to(torch.float32)).add_(r)
+        rr.copy_(rr_new)
+        k_dev.add_(1)
+        hist.index_copy_(0, k_dev.view(1), torch.sqrt(rr / bb).view(1))
+
+    if graph:
+        # capture one iteration (after a warm-up on a side stream) and replay it
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        saved = (x.clone(), r.clone(), p.clone(), rr.clone(), hist.clone(), k_dev.clone())
+        with torch.cuda.stream(s):
+            step()
+        torch.cuda.current_stream().wait_stream(s)
+        x.copy_(saved[0]); r.copy_(saved[1]); p.copy_(saved[2]); rr.copy_(saved[3])
+        hist.copy_(saved[4]); k_dev.copy_(saved[5])
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            step()
+        for _ in range(maxiter):
+            g.replay()
+        its = maxiter
+    else:
+        its = 0
+        for _ in range(maxiter):
+            step()
+            its += 1
+            if tol > 0 and float(hist[its]) <= tol:
+                break
+    return CGResult(x, its, hist[: its + 1].cpu().tolist())

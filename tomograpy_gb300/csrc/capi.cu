@@ -90,6 +90,10 @@ tg_status project_views(const tg_map_header *mh, const tg_image_header *views, i
   if (obstacle != TG_OBSTACLE_NONE && obstacle != TG_OBSTACLE_SUN)
     return fail(TG_EINVAL, "obstacle must be none or sun");
   if (dtype != TG_F32 && dtype != TG_F64) return fail(TG_EINVAL, "data dtype must be f32 or f64");
+  if (count <= 0 || n1 == 0 || n2 == 0) {
+    if (n1 < 0 || n2 < 0 || n_views < 0) return fail(TG_EINVAL, "negative size");
+    return TG_OK;  // nothing to trace (an empty stack may come with NULL pointers)
+  }
   if (!data || !map) return fail(TG_EINVAL, "data or map pointer is NULL");
   const bool four_d = (mode == TG_PJT || mode == TG_BPJT);
   tg::Geometry G;
@@ -100,16 +104,17 @@ tg_status project_views(const tg_map_header *mh, const tg_image_header *views, i
   if (count <= 0 || n1 == 0 || n2 == 0) return TG_OK;
   cudaStream_t s = (cudaStream_t)stream;
   int gx, gy;
+  const int rows = (dtype == TG_F32) ? tg::kFastRows : tg::kRows;
   if (ray_i >= 0) {
     G.ray_i = ray_i;
     G.ray_j = ray_j;
     G.mask_eq1 = 1;
     G.bx0 = ray_j / 32;
-    G.by0 = ray_i / tg::kRows;
+    G.by0 = ray_i / rows;
     gx = gy = 1;
   } else {
     gx = (int)((n2 + 31) / 32);
-    gy = (int)((n1 + tg::kRows - 1) / tg::kRows);
+    gy = (int)((n1 + rows - 1) / rows);
     if (gy > 65535) return fail(TG_EUNSUPPORTED, "image has too many rows (%lld)", (long long)n1);
   }
   for (int32_t v = 0; v < count; v += 65535) {
@@ -247,7 +252,7 @@ tg_status tg_conic_full_backprojector_deterministic(
   // accumulator offsets are dense C order (n0, n1, n2) within a frame
   const double span = (double)G.n[0] * G.n[1] * G.n[2];
   idx64 = span >= 2147483647.0;
-  const int gx = (int)((n2 + 31) / 32), gy = (int)((n1 + tg::kRows - 1) / tg::kRows);
+  const int gx = (int)((n2 + 31) / 32), gy = (int)((n1 + tg::kFastRows - 1) / tg::kFastRows);
   if (gy > 65535) return fail(TG_EUNSUPPORTED, "image has too many rows");
   if (n_views > 65535) return fail(TG_EUNSUPPORTED, "deterministic mode takes at most 65535 views per call");
   G.view0 = 0;
@@ -271,7 +276,7 @@ tg_status tg_segment_counts(const tg_map_header *map_header, const tg_image_head
                                mask_dtype, mask_strides, false, &idx64);
   if (st != TG_OK) return st;
   if (n_views == 0 || n1 == 0 || n2 == 0) return TG_OK;
-  const int gx = (int)((n2 + 31) / 32), gy = (int)((n1 + tg::kRows - 1) / tg::kRows);
+  const int gx = (int)((n2 + 31) / 32), gy = (int)((n1 + tg::kFastRows - 1) / tg::kFastRows);
   if (gy > 65535) return fail(TG_EUNSUPPORTED, "image has too many rows");
   for (int32_t v = 0; v < n_views; v += 65535) {
     G.view0 = v;
@@ -280,6 +285,16 @@ tg_status tg_segment_counts(const tg_map_header *map_header, const tg_image_head
     if (e != cudaSuccess) return launch_status(e, "segment count launch");
   }
   return TG_OK;
+}
+
+size_t tg_dot_workspace_bytes(void) { return 1216 * sizeof(double); }
+
+tg_status tg_dot_f32(const float *a, const float *b, int64_t n, double *out, void *workspace, size_t workspace_bytes,
+                     void *stream) {
+  if (!a || !b || !out || n < 0) return fail(TG_EINVAL, "bad dot arguments");
+  if (!workspace || workspace_bytes < tg_dot_workspace_bytes() || ((uintptr_t)workspace & 7u))
+    return fail(TG_ENOMEM, "dot workspace needs %zu bytes, 8-byte aligned", tg_dot_workspace_bytes());
+  return launch_status(tg::launch_dot(a, b, n, (double *)workspace, out, (cudaStream_t)stream), "dot launch");
 }
 
 const char *tg_last_error(void) { return g_err; }

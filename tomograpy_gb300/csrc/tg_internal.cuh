@@ -14,6 +14,10 @@ namespace tg {
 // its 32 rays walk neighbouring voxels of the cube's fastest axis.
 constexpr int kRows = 8;
 constexpr int kThreads = 32 * kRows;
+// The fast kernels give each warp kFastRowsPerWarp rows, so a CTA's
+// per-tile trigonometry serves kFastRows x 32 rays.
+constexpr int kFastRowsPerWarp = 2;
+constexpr int kFastRows = kRows * kFastRowsPerWarp;
 
 // The reference's finite "infinity" for zero direction components
 // (tomograpy/C_siddon.c.template:17).
@@ -71,5 +75,7 @@ cudaError_t launch_intersection_parameters(const Geometry &G, int ctype_f64, con
 cudaError_t launch_deterministic_bpj(const Geometry &G, int mode, int obstacle, bool idx64, const float *data,
                                      float *map, void *workspace, int grid_x, int grid_y, int grid_z,
                                      cudaStream_t s);
+
+cudaError_t launch_dot(const float *a, const float *b, long long n, double *partial, double *out, cudaStream_t s);
 
 }  // namespace tg

@@ -52,14 +52,14 @@ class Siddon(LinearOperator):
             if "R1_1" not in h:
                 S.H.header_rotation_matrix(h)
         h0 = self.data_header[0]
-        self.n1, self.n2, self.T = int(h0["NAXIS1"]), int(h0["NAXIS2"]), len(self.data_header)
+        self.n1, self.n2, self.n_views = int(h0["NAXIS1"]), int(h0["NAXIS2"]), len(self.data_header)
         if cube_shape is None:
             cube_shape = tuple(int(self.map_header["NAXIS%d" % (k + 1)]) for k in range(3))
         self.cube_shape = tuple(int(v) for v in cube_shape)
         self.four_d = len(self.cube_shape) == 4
         self.frames = None
         if self.four_d:
-            fr = np.arange(self.T) if frames is None else np.asarray(frames)
+            fr = np.arange(self.n_views) if frames is None else np.asarray(frames)
             if fr.min() < 0 or fr.max() >= self.cube_shape[3]:
                 raise ValueError("view frame index outside the cube's frames")
             self.frames = fr
@@ -71,7 +71,7 @@ class Siddon(LinearOperator):
         self.obstacle = obstacle
         self.deterministic = deterministic
         self._workspace = None
-        self.data_shape = (self.n1, self.n2, self.T)
+        self.data_shape = (self.n1, self.n2, self.n_views)
         n_in = int(np.prod(self.cube_shape))
         n_out = int(np.prod(self.data_shape))
         super().__init__(dtype=np.dtype(dtype), shape=(n_out, n_in))
@@ -89,7 +89,7 @@ class Siddon(LinearOperator):
         tensor, or fills ``out`` (device or host tensor) and returns it."""
         xd = self._dev(x, self.cube_shape)
         y = torch.zeros(self.data_shape, dtype=self.tdtype, device=self.device)
-        S.run_device("pjt" if self.four_d else "pj", y, xd, self.views_dev, self.mh, self.T, self.mask,
+        S.run_device("pjt" if self.four_d else "pj", y, xd, self.views_dev, self.mh, self.n_views, self.mask,
                      self.obstacle)
         return self._out(y, out)
 
@@ -103,10 +103,10 @@ class Siddon(LinearOperator):
                 _lib.i64(list(self.cube_shape) + ([] if self.four_d else [1])))
             if self._workspace is None or self._workspace.numel() < need:
                 self._workspace = torch.empty(need, dtype=torch.uint8, device=self.device)
-            S.run_device("bpjt" if self.four_d else "bpj", yd, x, self.views_dev, self.mh, self.T, self.mask,
+            S.run_device("bpjt" if self.four_d else "bpj", yd, x, self.views_dev, self.mh, self.n_views, self.mask,
                          self.obstacle, deterministic=True, workspace=self._workspace)
         else:
-            S.run_device("bpjt" if self.four_d else "bpj", yd, x, self.views_dev, self.mh, self.T, self.mask,
+            S.run_device("bpjt" if self.four_d else "bpj", yd, x, self.views_dev, self.mh, self.n_views, self.mask,
                          self.obstacle)
         return self._out(x, out)
 

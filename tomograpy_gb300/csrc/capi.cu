@@ -90,18 +90,15 @@ tg_status project_views(const tg_map_header *mh, const tg_image_header *views, i
   if (obstacle != TG_OBSTACLE_NONE && obstacle != TG_OBSTACLE_SUN)
     return fail(TG_EINVAL, "obstacle must be none or sun");
   if (dtype != TG_F32 && dtype != TG_F64) return fail(TG_EINVAL, "data dtype must be f32 or f64");
-  if (count <= 0 || n1 == 0 || n2 == 0) {
-    if (n1 < 0 || n2 < 0 || n_views < 0) return fail(TG_EINVAL, "negative size");
-    return TG_OK;  // nothing to trace (an empty stack may come with NULL pointers)
-  }
-  if (!data || !map) return fail(TG_EINVAL, "data or map pointer is NULL");
   const bool four_d = (mode == TG_PJT || mode == TG_BPJT);
   tg::Geometry G;
   bool idx64 = false;
   tg_status st = make_geometry(G, mh, views, n_views, n1, n2, ds, map_shape, ms, mask, mask_dtype, ks, four_d,
                                &idx64);
   if (st != TG_OK) return st;
+  // nothing to trace: an empty stack may come with NULL data / cube pointers
   if (count <= 0 || n1 == 0 || n2 == 0) return TG_OK;
+  if (!data || !map) return fail(TG_EINVAL, "data or map pointer is NULL");
   cudaStream_t s = (cudaStream_t)stream;
   int gx, gy;
   const int rows = (dtype == TG_F32) ? tg::kFastRows : tg::kRows;

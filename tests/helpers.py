@@ -6,9 +6,12 @@ Tolerances (float32 GPU path against the float64 reference / oracle):
 * images: per-pixel max relative error <= 1e-5 over pixels whose reference
   value is >= 1e-3 of the image maximum and whose ray is not degenerate, and
   normwise error max|dy| / max|y| <= 1e-5 over all non-degenerate pixels;
-* backprojected cubes: per-voxel max relative error <= 1e-4 over voxels >= 1e-3
+* backprojected cubes: per-voxel max relative error <= 1e-4 over voxels >= 1e-2
   of the cube maximum, normwise <= 1e-4 (degenerate rays masked out of both
-  sides);
+  sides).  A voxel below 1% of the maximum is made of a few short corner
+  segments; a float32 segment length carries an absolute error of about one
+  float32 ulp of the ray parameter (~5e-7 radii at the far side of a 3-radii
+  cube), which is not small relative to such a voxel;
 * adjoint: |<Px, y> - <x, P^T y>| / |<Px, y>| <= 1e-5.
 
 A ray is *degenerate* when a component of its direction is non-zero but
@@ -30,6 +33,7 @@ CUBE_KEYS = ["CDELT1", "CDELT2", "CDELT3", "PSHAPE1", "PSHAPE2", "PSHAPE3",
 
 IMG_TOL = 1e-5
 CUBE_TOL = 1e-4
+CUBE_SIG = 1e-2
 ADJ_TOL = 1e-5
 
 _golden = None
@@ -84,8 +88,10 @@ def degenerate_rays(views, n1, n2):
     return np.any((a > 0) & (a < 1e-12), axis=-1)
 
 
-def image_errors(y, ref, exclude=None):
-    """(per-pixel max relative over significant pixels, normwise) errors."""
+def image_errors(y, ref, exclude=None, sig=1e-3):
+    """(per-element max relative error over elements >= sig * max|ref|,
+    normwise max|y - ref| / max|ref|).  Images use sig = 1e-3, cubes
+    CUBE_SIG."""
     y = np.asarray(y, np.float64)
     ref = np.asarray(ref, np.float64)
     keep = np.ones(ref.shape, bool) if exclude is None else ~exclude
@@ -94,8 +100,8 @@ def image_errors(y, ref, exclude=None):
         return 0.0, float(np.abs(y[keep]).max()) if keep.any() else 0.0
     d = np.abs(y - ref)
     norm = d[keep].max() / scale
-    sig = keep & (np.abs(ref) >= 1e-3 * scale)
-    rel = (d[sig] / np.abs(ref[sig])).max() if sig.any() else 0.0
+    big = keep & (np.abs(ref) >= sig * scale)
+    rel = (d[big] / np.abs(ref[big])).max() if big.any() else 0.0
     return float(rel), float(norm)
 
 

@@ -8,7 +8,7 @@ import pytest
 
 import oracle
 import tomograpy_gb300 as tg
-from helpers import (ADJ_TOL, CUBE_TOL, IMG_TOL, degenerate_rays, golden, golden_case, image_errors, rel_dot)
+from helpers import (ADJ_TOL, CUBE_SIG, CUBE_TOL, IMG_TOL, degenerate_rays, golden, golden_case, image_errors, rel_dot)
 from tomograpy_gb300 import synthetic
 from tomograpy_gb300.infoarray import InfoArray
 
@@ -67,7 +67,7 @@ def test_golden_backprojection(obstacle, dtype):
     ref = InfoArray(shape=(24, 24, 24), header=dict(ch))
     oracle.backprojector(InfoArray(data=y.astype(dtype).astype(np.float64), header=_hdrs(vh)), ref,
                          obstacle=obstacle)
-    rel, norm = image_errors(cube, ref)
+    rel, norm = image_errors(cube, ref, sig=CUBE_SIG)
     tol = CUBE_TOL if dtype == np.float32 else 1e-12
     assert rel <= tol and norm <= tol, (rel, norm)
 
@@ -131,7 +131,7 @@ def test_golden_time_dependent(obstacle, dtype):
     ref = InfoArray(shape=(12, 12, 12, 7), header=dict(ch))
     oracle.backprojector4d(InfoArray(data=y.astype(dtype).astype(np.float64), header=_hdrs(vh)), ref,
                            obstacle=obstacle)
-    rel, norm = image_errors(cube, ref)
+    rel, norm = image_errors(cube, ref, sig=CUBE_SIG)
     assert norm <= (CUBE_TOL if dtype == np.float32 else 1e-12), (rel, norm)
 
 
@@ -269,7 +269,7 @@ def _compare_pj_bpj(ch, vh, x, y, obstacle, shape_img):
     tg.backprojector(InfoArray(data=yy, header=_hdrs(vh)), cube, obstacle=obstacle)
     cref = InfoArray(shape=x.shape, header=dict(ch))
     oracle.backprojector(InfoArray(data=yy.astype(np.float64), header=_hdrs(vh)), cref, obstacle=obstacle)
-    rel, norm = image_errors(cube, cref)
+    rel, norm = image_errors(cube, cref, sig=CUBE_SIG)
     assert rel <= CUBE_TOL and norm <= CUBE_TOL, ("bpj", rel, norm)
 
 
@@ -382,7 +382,7 @@ def test_deterministic_backprojection():
     np.testing.assert_array_equal(outs[0], outs[1])
     ref = InfoArray(shape=(48, 48, 48), header=dict(ch))
     oracle.backprojector(InfoArray(data=y.astype(np.float64), header=_hdrs(vh)), ref, obstacle="sun")
-    rel, norm = image_errors(outs[0], ref)
+    rel, norm = image_errors(outs[0], ref, sig=CUBE_SIG)
     assert rel <= CUBE_TOL and norm <= CUBE_TOL, (rel, norm)
 
 

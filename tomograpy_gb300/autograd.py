@@ -89,7 +89,7 @@ def reconstruct_lbfgs(op, y, iters=50, tv=1e-3, eps=1e-6, z0=None, scale=None, h
         r = project(x, op) - y
         loss = 0.5 * (r.double() ** 2).sum() / norm + tv * tv_smooth(x / scale, eps).double() / x.numel()
         loss.backward()
-        losses.append(float(loss))
+        losses.append(float(loss.detach()))
         return loss
 
     opt.step(closure)

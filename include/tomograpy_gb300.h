@@ -146,6 +146,27 @@ tg_status tg_conic_full_backprojector_deterministic(
     const int64_t map_strides[4], const void *mask, tg_dtype mask_dtype, const int64_t mask_strides[3],
     int32_t obstacle, int32_t mode, void *workspace, size_t workspace_bytes, void *stream);
 
+/* Deterministic backprojection without any device allocation, for callers
+ * that cannot allocate device memory: hosts that own all device memory through
+ * their own allocator or budget and do not let a plug-in call cudaMalloc
+ * (which also synchronises the device), and FFI callers that reach only this C
+ * ABI.  No counterpart in the reference.  Same arguments and result as
+ * tg_conic_full_backprojector_deterministic, but the scratch is a fixed array
+ * inside the library of tg_noalloc_scratch_bytes() bytes (32 MiB, held on
+ * every GPU that loads the library until the process exits), which limits the
+ * cube to (32 MiB - 256 B) / 8 = 4,194,272 voxels (n0*n1*n2, times the frame
+ * count for TG_BPJT); larger cubes are rejected with TG_ENOMEM.  The first
+ * call on a device looks up the scratch address (cudaGetSymbolAddress) with
+ * that device current, so make it before any stream capture.  Every call
+ * shares the scratch and clears it first: calls that overlap on the GPU
+ * (different streams or host threads) race. */
+size_t tg_noalloc_scratch_bytes(void);
+tg_status tg_conic_full_backprojector_deterministic_noalloc(
+    const tg_map_header *map_header, const tg_image_header *views, int32_t n_views, float *data, int64_t n1,
+    int64_t n2, const int64_t data_strides[3], float *map, const int64_t map_shape[4],
+    const int64_t map_strides[4], const void *mask, tg_dtype mask_dtype, const int64_t mask_strides[3],
+    int32_t obstacle, int32_t mode, void *stream);
+
 /* Number of voxel segments the f32 kernel accumulates along each ray, added
  * as float into counts (n1, n2, n_views) with strides count_strides[3].  A
  * diagnostic with no counterpart in the reference: it gives the exact

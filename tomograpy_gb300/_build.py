@@ -23,6 +23,7 @@ UNITS = {
     "siddon_ref.cu": ["--fmad=false"],
     "deterministic.cu": [],
     "reduce.cu": [],
+    "noalloc.cu": [],
     "capi.cu": [],
 }
 

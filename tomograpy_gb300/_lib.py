@@ -61,6 +61,11 @@ def load(build_if_missing=True):
     L.tg_conic_full_backprojector_deterministic.argtypes = proj_args[:3] + [P, I64, I64, P, P, P, P, P, I32, P,
                                                                             I32, I32, P, SZ, P]
     L.tg_segment_counts.argtypes = [P, P, I32, P, I64, I64, P, P, P, I32, P, I32, P]
+    L.tg_noalloc_scratch_bytes.argtypes = []
+    L.tg_noalloc_scratch_bytes.restype = SZ
+    L.tg_conic_full_backprojector_deterministic_noalloc.argtypes = proj_args[:3] + [P, I64, I64, P, P, P, P, P,
+                                                                                    I32, P, I32, I32, P]
+    L.tg_conic_full_backprojector_deterministic_noalloc.restype = ctypes.c_int
     L.tg_dot_workspace_bytes.argtypes = []
     L.tg_dot_workspace_bytes.restype = SZ
     L.tg_dot_f32.argtypes = [P, P, I64, P, P, SZ, P]

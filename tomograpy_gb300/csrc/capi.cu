@@ -284,6 +284,32 @@ tg_status tg_segment_counts(const tg_map_header *map_header, const tg_image_head
   return TG_OK;
 }
 
+size_t tg_noalloc_scratch_bytes(void) { return tg::noalloc_scratch_bytes(); }
+
+tg_status tg_conic_full_backprojector_deterministic_noalloc(
+    const tg_map_header *map_header, const tg_image_header *views, int32_t n_views, float *data, int64_t n1,
+    int64_t n2, const int64_t data_strides[3], float *map, const int64_t map_shape[4], const int64_t map_strides[4],
+    const void *mask, tg_dtype mask_dtype, const int64_t mask_strides[3], int32_t obstacle, int32_t mode,
+    void *stream) {
+  if (mode != TG_BPJ && mode != TG_BPJT) return fail(TG_EINVAL, "deterministic mode is for bpj / bpjt");
+  if (!map_shape) return fail(TG_EINVAL, "map shape is NULL");
+  const bool four_d = (mode == TG_BPJT);
+  const int64_t shape4[4] = {map_shape[0], map_shape[1], map_shape[2], four_d ? map_shape[3] : 1};
+  const size_t need = tg_deterministic_workspace_bytes(shape4);
+  if (need > tg::noalloc_scratch_bytes())
+    return fail(TG_ENOMEM,
+                "cube of %lld x %lld x %lld x %lld voxels needs %zu bytes of scratch; the built-in scratch holds "
+                "%zu bytes (%zu voxels): use tg_conic_full_backprojector_deterministic with a workspace",
+                (long long)shape4[0], (long long)shape4[1], (long long)shape4[2], (long long)shape4[3], need,
+                tg::noalloc_scratch_bytes(), (tg::noalloc_scratch_bytes() - 256) / 8);
+  void *scratch = nullptr;
+  cudaError_t e = tg::noalloc_scratch(&scratch);
+  if (e != cudaSuccess) return launch_status(e, "scratch address lookup");
+  return tg_conic_full_backprojector_deterministic(map_header, views, n_views, data, n1, n2, data_strides, map,
+                                                   map_shape, map_strides, mask, mask_dtype, mask_strides, obstacle,
+                                                   mode, scratch, tg::noalloc_scratch_bytes(), stream);
+}
+
 size_t tg_dot_workspace_bytes(void) { return 1216 * sizeof(double); }
 
 tg_status tg_dot_f32(const float *a, const float *b, int64_t n, double *out, void *workspace, size_t workspace_bytes,

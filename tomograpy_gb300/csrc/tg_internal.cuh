@@ -76,6 +76,8 @@ cudaError_t launch_deterministic_bpj(const Geometry &G, int mode, int obstacle, 
                                      float *map, void *workspace, int grid_x, int grid_y, int grid_z,
                                      cudaStream_t s);
 
+cudaError_t noalloc_scratch(void **ptr);
+size_t noalloc_scratch_bytes();
 cudaError_t launch_dot(const float *a, const float *b, long long n, double *partial, double *out, cudaStream_t s);
 
 }  // namespace tg

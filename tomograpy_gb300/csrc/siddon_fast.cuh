@@ -16,11 +16,13 @@
 //    entry face) and the full double-precision reference set-up
 //    (siddon_geom.cuh) runs when that classification is within its error
 //    bound;
-//  * the voxel walk in single precision RELATIVE TO THE ENTRY POINT: the k-th
-//    plane crossing of family a is t = D_a + k * |p_a| (one FMA, no running
-//    sum), so crossing positions carry no accumulated drift and the
-//    catastrophic cancellation of the reference's float path
-//    (D[k] = next*p + a1 - amin with a1, amin ~ 215) never occurs.  Steps run
+//  * the voxel walk in single precision, measured from the chord's midpoint:
+//    the k-th plane crossing of family a is t = d_a + k * |p_a| (one FMA, no
+//    running sum) with k counted from the crossing nearest the midpoint and
+//    d_a, |p_a| derived from double-float values, so crossing positions carry
+//    no accumulated drift, their rounding scales with the distance from the
+//    midpoint, and the catastrophic cancellation of the reference's float
+//    path (D[k] = next*p + a1 - amin with a1, amin ~ 215) never occurs.  Steps run
 //    in batches of kBatch that are proven, by one bound, to start before the
 //    stop parameter, so a batch needs no per-step test and its kBatch cube
 //    gathers are issued together;
@@ -40,7 +42,28 @@
 
 namespace tg {
 
-constexpr int kBatch = 8;                  // steps per batch of independent gathers
+// Compile-time tuning per direction (measured on GB300 at 256^3 x 360 x 512^2:
+// the gather-bound projection prefers longer batches, the atomic-bound
+// backprojection more resident warps).
+#ifndef TG_PJ_BATCH
+#define TG_PJ_BATCH 8
+#endif
+#ifndef TG_PJ_MIN_BLOCKS
+#define TG_PJ_MIN_BLOCKS 3
+#endif
+#ifndef TG_BPJ_BATCH
+#define TG_BPJ_BATCH 4
+#endif
+#ifndef TG_BPJ_MIN_BLOCKS
+#define TG_BPJ_MIN_BLOCKS 4
+#endif
+__host__ __device__ constexpr bool is_backprojection(int mode) { return mode == TG_BPJ || mode == TG_BPJT; }
+// steps per batch of independent gathers / atomics
+__host__ __device__ constexpr int batch_steps(int mode) { return is_backprojection(mode) ? TG_BPJ_BATCH : TG_PJ_BATCH; }
+// CTAs per SM the register budget must allow
+__host__ __device__ constexpr int min_blocks(int mode) {
+  return is_backprojection(mode) ? TG_BPJ_MIN_BLOCKS : TG_PJ_MIN_BLOCKS;
+}
 constexpr float kSunTh = 1e-5f;            // single-precision |d - 1| decision threshold
 
 struct DetScale {                          // deterministic-mode scale factors (device)
@@ -51,61 +74,179 @@ struct DetScale {                          // deterministic-mode scale factors (
   unsigned int pad;
 };
 
-// Per-CTA tables: cos / sin of lambda for the 32 columns, and for each of the
-// kFastRows rows A = R . (cos gamma, sin gamma, 0), so that a ray's direction
-// R . (cos l cos g, cos l sin g, sin l) is cos l * A + sin l * R[:, 2].
+// Per-CTA tables.  A ray's direction R . (cos l cos g, cos l sin g, sin l) is
+// cos l * w with w = A_row + tan(l) R[:, 2], A_row = R . (cos g, sin g, 0);
+// the fast walk runs in the scaled parameter beta = alpha cos l along w and
+// rescales lengths by 1 / cos l.  A (per row) and tan l (per column) are
+// computed once per CTA in double precision and kept as hi + lo float pairs,
+// so the per-ray set-up is double-float arithmetic on the FP32 pipes.
 struct FastTables {
-  double cl[32], sl[32];
-  double A[kFastRows][3];
+  double cl[32], sl[32];               // cos / sin lambda per column
+  float th[32], tl[32];                // tan(lambda), hi + lo
+  float icl[32];                       // 1 / cos(lambda)
+  double A[kFastRows][3];              // R . (cos g, sin g, 0) per row
+  float ah[kFastRows][3], al[kFastRows][3];    // A, hi + lo
+  float B[3], Bl[3];                   // R[:, 2], hi + lo
+  float mh[3], ml[3];                  // M - MMIN, hi + lo
+  float fh[3][2], fl[3][2];            // F - M for the MMIN (0) / MMAX (1) face, hi + lo
 };
 
-__device__ __forceinline__ void fill_fast_tables(FastTables &T, const tg_image_header &V, int col0, int row0) {
+// Double-float helpers (pairs hi + lo of floats; error-free products by FMA).
+struct df {
+  float hi, lo;
+};
+
+__device__ __forceinline__ df df_from(float a, float b) {  // renormalise a + b
+  const float s = a + b;
+  return {s, b - (s - a)};
+}
+
+__device__ __forceinline__ df df_mul(df a, df b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+  return df_from(p, e);
+}
+
+__device__ __forceinline__ df df_add(df a, df b) {
+  const float s = a.hi + b.hi;
+  const float v = s - a.hi;
+  const float e = (a.hi - (s - v)) + (b.hi - v);  // two-sum error
+  return df_from(s, e + a.lo + b.lo);
+}
+
+__device__ __forceinline__ df df_rcp(df a) {  // 1 / a to ~2^-46
+  const float r = __frcp_rn(a.hi);
+  const float e = fmaf(-a.lo, r, fmaf(-a.hi, r, 1.f));
+  return df_from(r, r * e);
+}
+
+__device__ __forceinline__ double split_lo(double v, float hi) { return v - (double)hi; }
+
+__device__ __forceinline__ void fill_fast_tables(FastTables &T, const Geometry &G, const tg_image_header &V,
+                                                 int col0, int row0) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (warp == 0) {
     double s, c;
     sincos(pixel_angle(col0 + lane, V, 1), &s, &c);
     T.sl[lane] = s;
     T.cl[lane] = c;
+    const double tau = s / c;
+    T.th[lane] = (float)tau;
+    T.tl[lane] = (float)split_lo(tau, T.th[lane]);
+    T.icl[lane] = __frcp_rn((float)c);
+    if (lane < 3) {
+      const double B = V.R[3 * lane + 2];
+      T.B[lane] = (float)B;
+      T.Bl[lane] = (float)split_lo(B, T.B[lane]);
+      const double mm = V.M[lane] - G.mh.mmin[lane];
+      T.mh[lane] = (float)mm;
+      T.ml[lane] = (float)split_lo(mm, T.mh[lane]);
+      const double f0 = G.mh.mmin[lane] - V.M[lane], f1 = G.mh.mmax[lane] - V.M[lane];
+      T.fh[lane][0] = (float)f0;
+      T.fl[lane][0] = (float)split_lo(f0, T.fh[lane][0]);
+      T.fh[lane][1] = (float)f1;
+      T.fl[lane][1] = (float)split_lo(f1, T.fh[lane][1]);
+    }
   } else if (warp == 1 && lane < kFastRows) {
-    double s, c;
-    sincos(pixel_angle(row0 + lane, V, 0), &s, &c);
+    double sg, cg;
+    sincos(pixel_angle(row0 + lane, V, 0), &sg, &cg);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) T.A[lane][k] = __dadd_rn(__dmul_rn(V.R[3 * k], c), __dmul_rn(V.R[3 * k + 1], s));
+    for (int k = 0; k < 3; ++k) {
+      const double A = __dadd_rn(__dmul_rn(V.R[3 * k], cg), __dmul_rn(V.R[3 * k + 1], sg));
+      T.A[lane][k] = A;
+      T.ah[lane][k] = (float)A;
+      T.al[lane][k] = (float)split_lo(A, T.ah[lane][k]);
+    }
   }
 }
 
 // State of one ray's walk in the single-precision relative frame.
 template <typename IDX>
 struct Walk {
-  float t[3];   // next crossing of each plane family (relative to entry)
-  float d[3];   // first crossing
+  float t[3];   // next crossing of each plane family (walk parameter)
+  float d[3];   // crossing m = 0 of each family (the one nearest the chord midpoint)
   float pa[3];  // spacing of crossings
-  float m[3];   // crossings done (exact small integers)
-  int iv0[3];   // entry voxel
+  float m[3];   // index of the next crossing, counted from that one (exact integers)
+  int iv0[3];   // voxel index that goes with m = 0
   int upd[3];
   IDX st[3];    // offset change when crossing a plane of each family
   IDX off;      // current voxel offset
   float texit;  // parameter of the first crossing that leaves the cube
   float E[3];   // entry point (absolute)
-  float uf[3];  // direction (single precision)
+  float uf[3];  // direction of the walk parameter (w, or u on the exact path)
+  float lscale; // walk-parameter length -> path length (1 / cos l, or 1)
+  float t0;     // walk origin: parameters are measured from the chord midpoint
 };
+
+// The ray direction u in double precision (exact path and obstacle
+// confirmation): u = cos l A_row + sin l R[:, 2], components below 1e-14
+// taken as zero.
+__device__ __forceinline__ void ray_u(const FastTables &T, const tg_image_header &V, int lane, int slot,
+                                      double u[3]) {
+  const double cl = T.cl[lane], sl = T.sl[lane];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    u[k] = fma(cl, T.A[slot][k], sl * V.R[3 * k + 2]);
+    if (fabs(u[k]) < kSnapZero) u[k] = 0.0;
+  }
+}
+
+// Result of the exact (double-precision reference) set-up.
+struct ExactSetup {
+  int iv[3], upd[3];
+  float d[3], pa[3], uf[3], ef[3];
+  float dl[3], pl[3];  // low parts: D = d + dl, |p| = pa + pl
+};
+
+// Full double-precision reference set-up (ambiguous rays): walk in alpha.
+// Kept out of line and writing to its own struct, so the walk state of the
+// common path stays in registers.
+static __device__ __noinline__ bool exact_setup(const Geometry &G, const tg_image_header &V, const FastTables &T,
+                                                int lane, int slot, ExactSetup &X) {
+  const float kInf = __int_as_float(0x7f800000);
+  double u[3];
+  ray_u(T, V, lane, slot, u);
+  const double M[3] = {V.M[0], V.M[1], V.M[2]};
+  RefWalk rw;
+  if (!ref_setup(G.mh, G.n, M, u, rw)) return false;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    X.iv[k] = rw.iv[k];
+    X.upd[k] = rw.upd[k];
+    X.d[k] = X.upd[k] ? (float)rw.D[k] : kInf;
+    X.pa[k] = X.upd[k] ? (float)rw.pabs[k] : kInf;
+    X.dl[k] = X.upd[k] ? (float)(rw.D[k] - (double)X.d[k]) : 0.f;
+    X.pl[k] = X.upd[k] ? (float)(rw.pabs[k] - (double)X.pa[k]) : 0.f;
+    X.uf[k] = (float)u[k];
+    X.ef[k] = (float)__dsub_rn(__dadd_rn(M[k], __dmul_rn(rw.amin, u[k])), G.mh.mmin[k]);
+  }
+  return true;
+}
 
 // Per-ray set-up.  Returns false when the ray does not enter the cube (the
 // reference's loop would not run).  `sun_lo` receives the parameter up to which
 // no obstacle test is needed (+inf when the ray cannot reach the sphere).
 template <bool SUN, typename IDX>
-__device__ __forceinline__ bool setup_ray(const Geometry &G, const double M[3], const double u[3], Walk<IDX> &w,
-                                          float &sun_lo) {
+__device__ __forceinline__ bool setup_ray(const Geometry &G, const tg_image_header &V, const FastTables &T,
+                                          int lane, int slot, Walk<IDX> &w, float &sun_lo) {
   const float kInf = __int_as_float(0x7f800000);
+  const df tau = {T.th[lane], T.tl[lane]};
+  df wd[3];  // w in double-float
   float lo[3], hi[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    w.uf[k] = (float)u[k];
-    if (u[k] != 0.0) {
-      const float Mf = (float)M[k];
-      const float inv = __frcp_rn(w.uf[k]);
-      const float a = (G.mminf[k] - Mf) * inv;
-      const float b = (G.mmaxf[k] - Mf) * inv;
+    wd[k] = df_add({T.ah[slot][k], T.al[slot][k]}, df_mul(tau, {T.B[k], T.Bl[k]}));
+    float wk = wd[k].hi;
+    if (fabsf(wk) < 1e-14f) {  // in-plane (or within 1e-14 rad of it)
+      wk = 0.f;
+      wd[k] = {0.f, 0.f};
+    }
+    w.uf[k] = wk;
+    if (wk != 0.f) {
+      const float inv = __frcp_rn(wk);
+      const float a = T.fh[k][0] * inv;
+      const float b = T.fh[k][1] * inv;
       lo[k] = fminf(a, b);
       hi[k] = fmaxf(a, b);
     } else {
@@ -114,104 +255,168 @@ __device__ __forceinline__ bool setup_ray(const Geometry &G, const double M[3], 
     }
   }
   int kin = 0;
-  if (lo[1] > lo[kin]) kin = 1;
-  if (lo[2] > lo[kin]) kin = 2;
-  const float aminf = lo[kin];
+  float aminf = lo[0];
+  if (lo[1] > aminf) {
+    kin = 1;
+    aminf = lo[1];
+  }
+  if (lo[2] > aminf) {
+    kin = 2;
+    aminf = lo[2];
+  }
   const float second = fmaxf(kin == 0 ? lo[1] : lo[0], kin == 2 ? lo[1] : lo[2]);
   const float amaxf = fminf(hi[0], fminf(hi[1], hi[2]));
   const float tol = 4e-6f * (fabsf(aminf) + fabsf(amaxf)) + 1e-6f;
   if (amaxf - aminf < -tol) return false;  // clear miss
   int iv[3];
-  float ef[3];  // entry point relative to MMIN (single precision)
-  if (amaxf - aminf < tol || aminf - second < tol) {
-    // Ambiguous in single precision: grazing ray or edge / corner entry.
-    RefWalk rw;
-    if (!ref_setup(G.mh, G.n, M, u, rw)) return false;
+  float ef[3];  // entry point relative to MMIN
+  float pl[3], dl[3];  // low parts of the crossing spacing and of the first crossing
+  const float ukin = (kin == 0) ? w.uf[0] : ((kin == 1) ? w.uf[1] : w.uf[2]);
+  if (amaxf - aminf < tol || aminf - second < tol || ukin == 0.f) {
+    ExactSetup X;
+    if (!exact_setup(G, V, T, lane, slot, X)) return false;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      iv[k] = rw.iv[k];
-      w.upd[k] = rw.upd[k];
-      w.d[k] = w.upd[k] ? (float)rw.D[k] : kInf;
-      w.pa[k] = w.upd[k] ? (float)rw.pabs[k] : kInf;
-      ef[k] = (float)__dsub_rn(__dadd_rn(M[k], __dmul_rn(rw.amin, u[k])), G.mh.mmin[k]);
+      iv[k] = X.iv[k];
+      w.upd[k] = X.upd[k];
+      w.d[k] = X.d[k];
+      w.pa[k] = X.pa[k];
+      pl[k] = X.pl[k];
+      dl[k] = X.dl[k];
+      w.uf[k] = X.uf[k];
+      ef[k] = X.ef[k];
     }
+    w.lscale = 1.f;
   } else {
-    const double F = (u[kin] > 0.0) ? G.mh.mmin[kin] : G.mh.mmax[kin];
-    const double amin = __ddiv_rn(__dsub_rn(F, M[kin]), u[kin]);
+    // All arrays below are indexed with compile-time indices only (unrolled
+    // loops with k == kin tests): a run-time index would move the walk state
+    // to local memory.
+    w.lscale = T.icl[lane];
+    float wk = 0.f, fh = 0.f, fl = 0.f;
+    df wkd = {0.f, 0.f};
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      w.upd[k] = (u[k] > 0.0) ? 1 : ((u[k] < 0.0) ? -1 : 0);
-      w.pa[k] = w.upd[k] ? __fdiv_rn(G.cdeltf[k], fabsf(w.uf[k])) : kInf;
       if (k == kin) {
-        iv[k] = (w.upd[k] > 0) ? 0 : G.n[k] - 1;
+        wk = w.uf[k];
+        wkd = wd[k];
+        fh = (wk > 0.f) ? T.fh[k][0] : T.fh[k][1];
+        fl = (wk > 0.f) ? T.fl[k][0] : T.fl[k][1];
+      }
+    }
+    // beta_in = (F - M_kin) / w_kin in double-float (F = MMIN if w > 0 else MMAX)
+    const df bin = df_mul({fh, fl}, df_rcp(wkd));
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      w.upd[k] = (w.uf[k] > 0.f) ? 1 : ((w.uf[k] < 0.f) ? -1 : 0);
+      // |p| = CDELT / |w| in double-float: its rounding would otherwise shift
+      // every crossing of the family by a fraction 2^-24 of its distance
+      // from the entry point
+      w.pa[k] = kInf;
+      pl[k] = 0.f;
+      dl[k] = 0.f;
+      if (w.upd[k]) {
+        const df aw = (wd[k].hi > 0.f) ? wd[k] : df{-wd[k].hi, -wd[k].lo};
+        const df pd = df_mul({G.cdeltf[k], G.cdeltl[k]}, df_rcp(aw));
+        w.pa[k] = pd.hi;
+        pl[k] = pd.lo;
+      }
+      if (k == kin) {
+        iv[k] = (wk > 0.f) ? 0 : G.n[k] - 1;
         w.d[k] = w.pa[k];
-        ef[k] = (w.upd[k] > 0) ? 0.f : (float)G.mh.pshape[k];
+        dl[k] = pl[k];
+        ef[k] = (wk > 0.f) ? 0.f : (float)G.mh.pshape[k];
       } else if (w.upd[k] == 0) {
         // In-plane ray: the index holds for the whole chord, so it is taken
         // exactly as the reference computes it (:783-786).
-        const double ep = __dsub_rn(M[k], G.mh.mmin[k]);
+        const double ep = __dsub_rn(V.M[k], G.mh.mmin[k]);
         iv[k] = ref_utrunc(__ddiv_rn(ep, G.mh.cdelt[k])) - ref_utrunc(__ddiv_rn(ep, G.mh.pshape[k]));
         w.d[k] = kInf;
         ef[k] = (float)ep;
       } else {
-        // Entry point on this axis, then floor division by CDELT; an index
-        // off by one at a plane only adds a zero-length first segment.
-        const double ep = fma(amin, u[k], __dsub_rn(M[k], G.mh.mmin[k]));
-        const double q = floor(ep * G.inv_cdelt[k]);
-        float r = (float)fma(-q, G.mh.cdelt[k], ep);
+        // E_k - MMIN_k = (M_k - MMIN_k) + beta_in w_k in double-float (the
+        // cancellation of the two ~d-sized terms leaves ~1e-11 radii), then
+        // the remainder against the exact plane position q * CDELT.
+        const df e = df_add({T.mh[k], T.ml[k]}, df_mul(bin, wd[k]));
+        const float C = G.cdeltf[k];
+        const float q = floorf((e.hi + e.lo) * G.inv_cdeltf[k]);
+        float r = fmaf(-q, C, e.hi) + fmaf(-q, G.cdeltl[k], e.lo);
         int qi = (int)q;
         if (r < 0.f) {
           qi -= 1;
-          r += G.cdeltf[k];
-        } else if (r >= G.cdeltf[k]) {
+          r += C;
+        } else if (r >= C) {
           qi += 1;
-          r -= G.cdeltf[k];
+          r -= C;
         }
         // the reference truncates: a point just outside the first / last
         // voxel still maps to it (:785-786)
         if (qi == -1) {
           qi = 0;
-          r -= G.cdeltf[k];
+          r -= C;
         } else if (qi == G.n[k]) {
           qi = G.n[k] - 1;
-          r += G.cdeltf[k];
+          r += C;
         }
         iv[k] = qi;
-        w.d[k] = (w.upd[k] > 0) ? __fdiv_rn(G.cdeltf[k] - r, w.uf[k]) : __fdiv_rn(r, -w.uf[k]);
-        ef[k] = (float)ep;
+        w.d[k] = (w.upd[k] > 0) ? __fdiv_rn(C - r, w.uf[k]) : __fdiv_rn(r, -w.uf[k]);
+        ef[k] = e.hi + e.lo;
       }
     }
   }
-  float texit = kInf;
+  float texit0 = kInf;
+  float ce[3];  // crossings of each family until its index leaves the cube
   IDX off = 0;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     if (iv[k] < 0 || iv[k] >= G.n[k]) return false;  // reference: in_map fails at once
     w.iv0[k] = iv[k];
-    w.t[k] = w.d[k];
     w.m[k] = 0.f;
     w.st[k] = (IDX)w.upd[k] * (IDX)G.ms[k];
     off += (IDX)iv[k] * (IDX)G.ms[k];
-    if (w.upd[k] != 0) {
-      const int cexit = (w.upd[k] > 0) ? G.n[k] - iv[k] : iv[k] + 1;
-      texit = fminf(texit, fmaf((float)(cexit - 1), w.pa[k], w.d[k]));
-    }
+    ce[k] = (float)((w.upd[k] > 0) ? G.n[k] - iv[k] : iv[k] + 1);
+    if (w.upd[k] != 0) texit0 = fminf(texit0, fmaf(ce[k] - 1.f, w.pa[k], w.d[k]));
     w.E[k] = G.mminf[k] + ef[k];
   }
   w.off = off;
+  // Re-origin the walk at the chord's midpoint h, and count each family's
+  // crossings from the one nearest to it (m0): crossing m of family a is
+  // then t = fma(m - m0, p, d'') with d'' = D + m0 (p + pl) - h evaluated
+  // with an exact product (|d''| <= |p|), so a crossing's rounding error
+  // scales with its distance from the midpoint instead of from the entry
+  // point.  The exit parameter is computed from the same values with the
+  // walk's own FMA, so the stop stays exact.
+  const float h = 0.5f * texit0;
+  w.t0 = -h;
+  float texit = kInf;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    w.t[k] = kInf;
+    if (w.upd[k] != 0) {
+      const float m0 = fminf(fmaxf(rintf(__fdividef(h - w.d[k], w.pa[k])), 0.f), ce[k] - 1.f);
+      const float p = m0 * w.pa[k];
+      const float e = fmaf(m0, w.pa[k], -p) + fmaf(m0, pl[k], dl[k]);
+      w.d[k] = ((p - h) + e) + w.d[k];
+      w.m[k] = -m0;
+      w.iv0[k] += w.upd[k] * (int)m0;
+      w.t[k] = fmaf(-m0, w.pa[k], w.d[k]);
+      texit = fminf(texit, fmaf(ce[k] - 1.f - m0, w.pa[k], w.d[k]));
+    }
+  }
   w.texit = texit;
   sun_lo = kInf;
   if (SUN) {
+    // |E + s dir|^2 = 1:  s^2 |dir|^2 + 2 s (E.dir) + |E|^2 - 1 = 0
+    const float ww = fmaf(w.uf[0], w.uf[0], fmaf(w.uf[1], w.uf[1], w.uf[2] * w.uf[2]));
     const float b = fmaf(w.E[0], w.uf[0], fmaf(w.E[1], w.uf[1], w.E[2] * w.uf[2]));
     const float c = fmaf(w.E[0], w.E[0], fmaf(w.E[1], w.E[1], w.E[2] * w.E[2])) - 1.f;
-    const float disc = fmaf(b, b, -c);
+    const float disc = fmaf(b, b, -ww * c);
     if (c < 1e-4f) {
       sun_lo = -kInf;  // entry at / inside the sphere: test from the start
-    } else if (b < 0.f && disc > -2e-5f) {
+    } else if (b < 0.f && disc > -2e-5f * ww) {
       const float sq = sqrtf(fmaxf(disc, 0.f));
-      const float s1 = -b - sq;
+      const float s1 = __fdividef(-b - sq, ww);
       const float g = 1e-5f + __fdividef(1e-5f, sq);
-      sun_lo = (sq > 0.f) ? s1 - g : -kInf;
+      sun_lo = (sq > 0.f) ? s1 - g - h : -kInf;
     }
   }
   return true;
@@ -221,8 +426,11 @@ __device__ __forceinline__ bool setup_ray(const Geometry &G, const double M[3], 
 // (the reference's |M + ac u0|^2 > 1 with ac the entry parameter of the
 // voxel): the entry parameter is the largest of the crossing parameters of the
 // voxel's lower planes along the ray.
-static __device__ __noinline__ bool exact_outside(const Geometry &G, const double M[3], const double u[3],
-                                                  const int iv[3]) {
+static __device__ __noinline__ bool exact_outside(const Geometry &G, const tg_image_header &V, const FastTables &T,
+                                                  int lane, int slot, const int iv[3]) {
+  double u[3];
+  ray_u(T, V, lane, slot, u);
+  const double M[3] = {V.M[0], V.M[1], V.M[2]};
   double ac = -1e300;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
@@ -237,9 +445,17 @@ static __device__ __noinline__ bool exact_outside(const Geometry &G, const doubl
 // One step of the walk: returns the segment length and the voxel offset it
 // belongs to, and advances the state.  Every plane family whose next crossing
 // equals the smallest advances (the reference's 2- and 3-way tie cases).
+// Smallest of three floats in one instruction (PTX three-input min, sm_100+);
+// a NaN operand is ignored like fminf does.
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
 template <typename IDX>
 __device__ __forceinline__ float walk_step(Walk<IDX> &w, float &cur, IDX &seg_off) {
-  const float tm = fminf(w.t[0], fminf(w.t[1], w.t[2]));
+  const float tm = min3f(w.t[0], w.t[1], w.t[2]);
   const float L = tm - cur;
   seg_off = w.off;
 #pragma unroll
@@ -298,35 +514,42 @@ __device__ __forceinline__ void trace_fast(const Geometry &G, const tg_image_hea
     yv = xin[po];
     if (yv == 0.f) return;  // adds exact zeros only
   }
-  const double M[3] = {V.M[0], V.M[1], V.M[2]};
-  double u[3];
-  const double cl = T.cl[lane], sl = T.sl[lane];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    u[k] = fma(cl, T.A[row_slot][k], sl * V.R[3 * k + 2]);
-    if (fabs(u[k]) < kSnapZero) u[k] = 0.0;
-  }
   Walk<IDX> w;
   float sun_lo;
-  if (!setup_ray<SUN, IDX>(G, M, u, w, sun_lo)) return;
+  if (!setup_ray<SUN, IDX>(G, V, T, lane, row_slot, w, sun_lo)) return;
+  yv *= w.lscale;  // lengths of the walk parameter -> path lengths
 
   const float *cin = PJ ? xin + fbase : nullptr;
   float *cout = PJ ? nullptr : xout + fbase;
   unsigned long long *aout = DET ? acc64 + fbase : nullptr;
-  const float yq = DET ? yv * dsc->yscale : 0.f;
+  const float yq = DET ? yv * dsc->yscale : 0.f;  // yv already carries lscale
   const float qs = DET ? dsc->qscale : 0.f;
+  // Projection sums are blocked: each batch (and the tail) sums its segments
+  // into `part`, which is then added to `acc`, so the float32 rounding grows
+  // with kBatch + steps / kBatch rather than with the step count.
   float acc = 0.f;
-  float cur = 0.f;
+  float cur = w.t0;
   const float tstop = fminf(w.texit, sun_lo);
   int guard = G.n[0] + G.n[1] + G.n[2] + 2;
 
-  // Batches of kBatch steps that are all known to start before tstop: the
-  // (kBatch-1)-th upcoming crossing is at most min_a(t_a + (kBatch-2) |p_a|).
+  // Why no step reads outside the cube: a step that starts at cur < texit
+  // reads a valid voxel.  The families advanced by the step before it had
+  // their crossing fma(m, p, d) = cur < texit <= fma(ce - 1, p, d) (texit is
+  // computed with the same FMA, see setup_ray), and fma(., p, d) is monotone
+  // in its first argument, so m < ce - 1 and the new index is still inside.
+  //
+  // Batches of kBatch steps: after j steps of a batch every family has
+  // advanced at most j times, so the start of step kBatch-1 (the crossing of
+  // step kBatch-2) is at most min_a fma(m_a + kBatch - 2, p_a, d_a).  When
+  // that bound is below tstop every step of the batch starts before tstop:
+  // the batch is exactly kBatch iterations of the single-step loop below, with
+  // no per-step test, and its kBatch cube gathers are issued together.
+  constexpr int kBatch = batch_steps(MODE);
   while (guard >= kBatch) {
-    const float bnd = fminf(fmaf((float)(kBatch - 2), w.pa[0], w.t[0]),
-                            fminf(fmaf((float)(kBatch - 2), w.pa[1], w.t[1]),
-                                  fmaf((float)(kBatch - 2), w.pa[2], w.t[2])));
-    if (!(bnd + fabsf(bnd) * 5e-7f < tstop)) break;
+    const float bnd = min3f(fmaf(w.m[0] + (float)(kBatch - 2), w.pa[0], w.d[0]),
+                            fmaf(w.m[1] + (float)(kBatch - 2), w.pa[1], w.d[1]),
+                            fmaf(w.m[2] + (float)(kBatch - 2), w.pa[2], w.d[2]));
+    if (!(bnd < tstop)) break;
     guard -= kBatch;
     float L[kBatch];
     IDX o[kBatch];
@@ -338,27 +561,31 @@ __device__ __forceinline__ void trace_fast(const Geometry &G, const tg_image_hea
       float v[kBatch];
 #pragma unroll
       for (int s = 0; s < kBatch; ++s) v[s] = __ldg(cin + o[s]);
+      float part = L[0] * v[0];
 #pragma unroll
-      for (int s = 0; s < kBatch; ++s) acc = fmaf(L[s], v[s], acc);
+      for (int s = 1; s < kBatch; ++s) part = fmaf(L[s], v[s], part);
+      acc += part;
     } else {
 #pragma unroll
       for (int s = 0; s < kBatch; ++s) accumulate<MODE, DET, IDX>(L[s], o[s], cin, cout, aout, yv, yq, qs, acc);
     }
   }
   // Remaining steps before tstop, one at a time.
+  float part = 0.f;
   while (cur < tstop && guard > 0) {
     --guard;
     IDX o;
     const float L = walk_step(w, cur, o);
-    accumulate<MODE, DET, IDX>(L, o, cin, cout, aout, yv, yq, qs, acc);
+    accumulate<MODE, DET, IDX>(L, o, cin, cout, aout, yv, yq, qs, part);
   }
   // Obstacle zone: test each voxel entry before accumulating it.
   if (SUN && cur < w.texit) {
     while (cur < w.texit && guard > 0) {
       --guard;
-      const float px = fmaf(cur, w.uf[0], w.E[0]);
-      const float py = fmaf(cur, w.uf[1], w.E[1]);
-      const float pz = fmaf(cur, w.uf[2], w.E[2]);
+      const float se = cur - w.t0;  // distance from the entry point
+      const float px = fmaf(se, w.uf[0], w.E[0]);
+      const float py = fmaf(se, w.uf[1], w.E[1]);
+      const float pz = fmaf(se, w.uf[2], w.E[2]);
       const float dd = fmaf(px, px, fmaf(py, py, pz * pz)) - 1.f;
       bool outside;
       if (dd > kSunTh) {
@@ -369,37 +596,48 @@ __device__ __forceinline__ void trace_fast(const Geometry &G, const tg_image_hea
         int ivn[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) ivn[k] = w.iv0[k] + w.upd[k] * (int)w.m[k];
-        outside = exact_outside(G, M, u, ivn);
+        outside = exact_outside(G, V, T, lane, row_slot, ivn);
       }
       if (!outside) break;
       IDX o;
       const float L = walk_step(w, cur, o);
-      accumulate<MODE, DET, IDX>(L, o, cin, cout, aout, yv, yq, qs, acc);
+      accumulate<MODE, DET, IDX>(L, o, cin, cout, aout, yv, yq, qs, part);
     }
   }
-  if (PJ && acc != 0.f) xout[po] += acc;
+  acc += part;
+  if (PJ && !CNT && acc != 0.f) xout[po] += acc * w.lscale;
+  if (CNT && acc != 0.f) xout[po] += acc;
+}
+
+// One CTA tile: rows [row0, row0 + 8 * RPW) x columns [col0, col0 + 32) of
+// view t; warp w traces rows w, w + 8, ... of the tile (RPW rows per warp).
+template <int MODE, bool SUN, typename IDX, bool DET, int RPW>
+__device__ __forceinline__ void tile_body(const Geometry &G, int t, int col0, int row0,
+                                          const float *__restrict__ xin, float *__restrict__ xout,
+                                          unsigned long long *__restrict__ acc64,
+                                          const DetScale *__restrict__ dsc) {
+  static_assert(RPW * kRows <= kFastRows, "tile taller than the CTA tables");
+  __shared__ FastTables T;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const tg_image_header &V = G.views[t];
+  fill_fast_tables(T, G, V, col0, row0);
+  __syncthreads();
+#pragma unroll 1
+  for (int r = 0; r < RPW; ++r) {
+    const int slot = warp + r * kRows;
+    trace_fast<MODE, SUN, IDX, DET>(G, V, T, row0 + slot, col0 + lane, t, slot, xin, xout, acc64, dsc);
+  }
 }
 
 // Modes: 0 = PJ, 1 = BPJ, 2 = PJT, 3 = BPJT, kModeCount; DET: backprojection
 // into the 64-bit fixed-point accumulator `acc64` instead of red.add.f32.
-// CTA: kFastRows rows x 32 columns of one view; warp w traces rows w and
-// w + kRows of the tile.
+// Grid (N2 / 32, N1 / kFastRows, views).
 template <int MODE, bool SUN, typename IDX, bool DET>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, min_blocks(MODE))
 fast_kernel(const Geometry G, const float *__restrict__ xin, float *__restrict__ xout,
             unsigned long long *__restrict__ acc64, const DetScale *__restrict__ dsc) {
-  __shared__ FastTables T;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int t = G.view0 + blockIdx.z;
-  const tg_image_header &V = G.views[t];
-  const int col0 = (G.bx0 + blockIdx.x) * 32, row0 = (G.by0 + blockIdx.y) * kFastRows;
-  fill_fast_tables(T, V, col0, row0);
-  __syncthreads();
-#pragma unroll 1
-  for (int r = 0; r < kFastRowsPerWarp; ++r) {
-    const int slot = warp + r * kRows;
-    trace_fast<MODE, SUN, IDX, DET>(G, V, T, row0 + slot, col0 + lane, t, slot, xin, xout, acc64, dsc);
-  }
+  tile_body<MODE, SUN, IDX, DET, kFastRowsPerWarp>(G, G.view0 + blockIdx.z, (G.bx0 + blockIdx.x) * 32,
+                                                   (G.by0 + blockIdx.y) * kFastRows, xin, xout, acc64, dsc);
 }
 
 }  // namespace tg

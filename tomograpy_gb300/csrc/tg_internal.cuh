@@ -16,7 +16,7 @@ constexpr int kRows = 8;
 constexpr int kThreads = 32 * kRows;
 // The fast kernels give each warp kFastRowsPerWarp rows, so a CTA's
 // per-tile trigonometry serves kFastRows x 32 rays.
-constexpr int kFastRowsPerWarp = 2;
+constexpr int kFastRowsPerWarp = 4;
 constexpr int kFastRows = kRows * kFastRowsPerWarp;
 
 // The reference's finite "infinity" for zero direction components
@@ -45,7 +45,7 @@ struct Geometry {
   int nframes;         // frames of a 4-D cube (1 for 3-D)
   long long ms[4];     // cube strides (elements)
   tg_map_header mh;
-  float cdeltf[3], mminf[3], mmaxf[3];
+  float cdeltf[3], cdeltl[3], mminf[3], mmaxf[3], inv_cdeltf[3];  // cdeltl: CDELT - (float)CDELT
   double inv_cdelt[3];
 };
 
@@ -76,6 +76,20 @@ cudaError_t launch_deterministic_bpj(const Geometry &G, int mode, int obstacle, 
                                      float *map, void *workspace, int grid_x, int grid_y, int grid_z,
                                      cudaStream_t s);
 
+cudaError_t launch_packed(const void *plan, int n_jobs, long long tiles, int rpw, bool idx64, int mode, int obstacle,
+                          cudaStream_t s);
+size_t packed_job_bytes();
+size_t packed_records_offset(int n_jobs);
+void packed_fill(void *dst, const Geometry &G, float *data, float *cube, long long tile0, int gx, int gy);
+cudaError_t launch_seg_dot(const float *a, const float *b, const long long *off, int n_seg, double *partial,
+                           double *out, cudaStream_t st);
+cudaError_t launch_seg_cg_x(float *x, float *r, const float *p, const float *Ap, const double *rr, const double *pAp,
+                            const long long *off, int n_seg, cudaStream_t st);
+cudaError_t launch_seg_cg_p(float *p, const float *r, double *rr, const double *rr_new, const long long *off,
+                            int n_seg, cudaStream_t st);
+size_t seg_workspace_bytes(int n_seg);
+cudaError_t launch_seg_axpby(float *y, const float *x, float alpha, float beta, const long long *off, int n_seg,
+                             cudaStream_t st);
 cudaError_t noalloc_scratch(void **ptr);
 size_t noalloc_scratch_bytes();
 cudaError_t launch_dot(const float *a, const float *b, long long n, double *partial, double *out, cudaStream_t s);

@@ -52,6 +52,9 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="one projection + one backprojection on the workload's geometry restricted to every "
+                         "10th view (36 views): the case the ncu summaries in profiles/ are captured on")
     return ap.parse_args()
 
 
@@ -346,8 +349,31 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_profile_case():
+    import torch
+
+    from tomograpy_gb300 import siddon, synthetic
+    cfg = synthetic.CONFIGS[WORKLOAD]
+    ch, vh = synthetic.make_geometry(WORKLOAD)
+    vh = vh[::10]
+    T, N, n = len(vh), cfg["N"], cfg["n"]
+    dev = torch.device("cuda")
+    x = torch.from_numpy(synthetic.phantom(ch, seed=0)).to(dev)
+    views = siddon.upload_views(vh, None, dev)
+    mh = siddon.pack_map_header(ch)
+    y = torch.zeros((T, N, N), device=dev).permute(1, 2, 0)
+    c = torch.zeros((n, n, n), device=dev)
+    siddon.run_device("pj", y, x, views, mh, T, obstacle="sun")
+    siddon.run_device("bpj", y, c, views, mh, T, obstacle="sun")
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": WORKLOAD, "views": T, "y_sum": float(y.sum()), "c_sum": float(c.sum())}))
+
+
 def main():
     args = parse()
+    if args.profile_case:
+        run_profile_case()
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

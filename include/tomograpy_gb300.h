@@ -185,6 +185,68 @@ size_t tg_dot_workspace_bytes(void);
 tg_status tg_dot_f32(const float *a, const float *b, int64_t n, double *out, void *workspace,
                      size_t workspace_bytes, void *stream);
 
+/* ---- Packed multi-job launches --------------------------------------------
+ * Many independent reconstructions traced by ONE kernel launch (no
+ * counterpart in the reference, which runs one projector call per stack).
+ * Describe each job with a tg_job, build a device plan once with
+ * tg_packed_plan (jobs are ordered by decreasing work; the plan keeps the
+ * device pointers, so reuse it while the buffers stay where they are), then
+ * launch tg_packed_projector(plan, info, mode, ...) -- e.g. once per CG
+ * iteration for every job.  rows_per_warp (1, 2 or 4) sets the CTA tile
+ * height (8 * rows_per_warp rows x 32 columns); pick it by timing (see
+ * tomograpy_gb300/batch.py). */
+typedef struct {
+  tg_map_header map_header;      /* cube header (host values) */
+  const tg_image_header *views;  /* device view table */
+  int32_t n_views;
+  int32_t reserved;
+  int64_t n1, n2;                /* image rows / columns */
+  int64_t data_strides[3];
+  int64_t map_shape[4];          /* map_shape[3] = frames (1 for 3-D) */
+  int64_t map_strides[4];
+  const void *mask;              /* NULL or device mask, type mask_dtype */
+  int64_t mask_strides[3];
+  int32_t mask_dtype;
+  int32_t reserved2;
+  float *data;                   /* device data stack (n1, n2, n_views) */
+  float *map;                    /* device cube */
+} tg_job;
+
+typedef struct {
+  int32_t n_jobs;
+  int32_t rows_per_warp;
+  int32_t four_d;
+  int32_t idx64;
+  int64_t tiles;                 /* CTAs of one packed launch */
+} tg_packed_info;
+
+size_t tg_packed_plan_bytes(int32_t n_jobs);
+tg_status tg_packed_plan(const tg_job *jobs, int32_t n_jobs, int32_t rows_per_warp, int32_t four_d, void *plan,
+                         size_t plan_bytes, tg_packed_info *info);
+tg_status tg_packed_projector(const void *plan, const tg_packed_info *info, int32_t mode, int32_t obstacle,
+                              void *stream);
+
+/* Segmented float64-accumulated inner products over float32 buffers:
+ * out[s] = sum_{i in [seg[2s], seg[2s+1])} a[i] b[i] for s < n_seg (seg:
+ * device int64[2 n_seg], element ranges that need not be contiguous or
+ * ordered); fixed reduction order.  Workspace of
+ * tg_segmented_workspace_bytes(n_seg) bytes. */
+size_t tg_segmented_workspace_bytes(int32_t n_seg);
+tg_status tg_segmented_dot_f32(const float *a, const float *b, const int64_t *seg, int32_t n_seg, double *out,
+                               void *workspace, size_t workspace_bytes, void *stream);
+/* Batched CG updates over the same segments, per segment s: alpha_s = rr[s] / pAp[s],
+ * x += alpha_s p, r -= alpha_s Ap (tg_cg_update_x); beta_s = rr_new[s] / rr[s],
+ * p = r + beta_s p, then rr[s] = rr_new[s] (tg_cg_update_p). */
+tg_status tg_cg_update_x(float *x, float *r, const float *p, const float *Ap, const double *rr, const double *pAp,
+                         const int64_t *seg, int32_t n_seg, void *stream);
+tg_status tg_cg_update_p(float *p, const float *r, double *rr, const double *rr_new, const int64_t *seg,
+                         int32_t n_seg, void *stream);
+
+/* y = alpha x + beta y over the segments (x may be NULL: y = beta y; with
+ * beta = 0, y = alpha x -- e.g. clearing a job's vectors or adding lam x). */
+tg_status tg_segmented_axpby(float *y, const float *x, float alpha, float beta, const int64_t *seg, int32_t n_seg,
+                             void *stream);
+
 /* Message for the last non-OK status returned on this thread. */
 const char *tg_last_error(void);
 

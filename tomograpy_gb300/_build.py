@@ -24,6 +24,7 @@ UNITS = {
     "deterministic.cu": [],
     "reduce.cu": [],
     "noalloc.cu": [],
+    "packed.cu": [],
     "capi.cu": [],
 }
 

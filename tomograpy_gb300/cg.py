@@ -9,7 +9,8 @@ a third-party package absent from the reference tree; this module restates
 textbook CG (Hestenes-Stiefel) for that system:
 
 * vectors in float32 on the device; inner products and residual norms
-  accumulated in float64 (``tg_dot_f32``, a fixed-order reduction);
+  accumulated in float64 (``tg_segmented_dot_f32``, a fixed-order
+  reduction), with the same kernels as the batched multi-job CG;
 * scalars (alpha, beta, residual norms) stay on the device as 0-d tensors, so
   an iteration needs no host synchronisation and can be captured once in a
   CUDA graph and replayed (``graph=True``).
@@ -86,35 +87,80 @@ class CGResult:
         self.residuals = residuals  # ||r_k|| / ||b||, float64 host list
 
 
+class SegmentOps:
+    """Inner products and CG vector updates over element ranges of flat
+    float32 buffers (``tg_segmented_dot_f32``, ``tg_cg_update_x``,
+    ``tg_cg_update_p``): one range for a single solve, one per job for the
+    batched solves, so both run the same arithmetic."""
+
+    def __init__(self, seg, device):
+        from .batch import _bind
+        self.L = _bind(_lib.load())
+        self.seg = seg if torch.is_tensor(seg) else torch.tensor(seg, dtype=torch.int64, device=device)
+        self.n = self.seg.numel() // 2
+        nb = max(8, self.L.tg_segmented_workspace_bytes(self.n))
+        self.ws = torch.empty(nb // 8, dtype=torch.float64, device=device)
+
+    @staticmethod
+    def _p(t):
+        return ctypes.c_void_p(t.data_ptr())
+
+    @staticmethod
+    def _st():
+        return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def dot(self, a, b, out):
+        _lib.check(self.L.tg_segmented_dot_f32(self._p(a), self._p(b), self._p(self.seg), self.n, self._p(out),
+                                               self._p(self.ws), self.ws.numel() * 8, self._st()))
+        return out
+
+    def update_x(self, x, r, p, Ap, rr, pAp):
+        _lib.check(self.L.tg_cg_update_x(self._p(x), self._p(r), self._p(p), self._p(Ap), self._p(rr),
+                                         self._p(pAp), self._p(self.seg), self.n, self._st()))
+
+    def update_p(self, p, r, rr, rr_new):
+        _lib.check(self.L.tg_cg_update_p(self._p(p), self._p(r), self._p(rr), self._p(rr_new), self._p(self.seg),
+                                         self.n, self._st()))
+
+    def axpby(self, y, x, alpha, beta):
+        _lib.check(self.L.tg_segmented_axpby(self._p(y), None if x is None else self._p(x), alpha, beta,
+                                             self._p(self.seg), self.n, self._st()))
+
+
 def cg(A, b, x0=None, maxiter=10, tol=0.0, graph=False):
     """Solve A x = b (A symmetric positive definite, callable on device tensors).
 
     Runs ``maxiter`` iterations (stopping early on the host only when
     ``tol`` > 0 and ``graph`` is False).  Returns a :class:`CGResult`.
+    Per iteration: alpha = rr / pAp, x += alpha p, r -= alpha Ap,
+    beta = rr_new / rr, p = r + beta p (scalars in float64 on the device,
+    vector updates as single float32 FMAs).
     """
     dev = b.device
-    dot = Dot(dev, n_slots=4)
+    if b.dtype != torch.float32 or not b.is_contiguous():
+        raise ValueError("cg takes a contiguous float32 right-hand side")
+    ops = SegmentOps([0, b.numel()], dev)
     x = torch.zeros_like(b) if x0 is None else x0.clone()
     r = b - A(x) if x0 is not None else b.clone()
     p = r.clone()
-    rr = dot(r, r, 0).clone()
-    bb = dot(b, b, 1).clone()
+    rr = torch.zeros(1, dtype=torch.float64, device=dev)
+    rr_new = torch.zeros_like(rr)
+    pAp = torch.zeros_like(rr)
+    bb = torch.zeros_like(rr)
+    ops.dot(r, r, rr)
+    ops.dot(b, b, bb)
     hist = torch.zeros(maxiter + 1, dtype=torch.float64, device=dev)
-    hist[0] = torch.sqrt(rr / bb)
+    hist[0] = torch.sqrt(rr / bb)[0]
     k_dev = torch.zeros((), dtype=torch.int64, device=dev)
 
     def step():
-        Ap = A(p)
-        pAp = dot(p, Ap, 2)
-        alpha = rr / pAp
-        x.add_(p * alpha.to(torch.float32))
-        r.sub_(Ap * alpha.to(torch.float32))
-        rr_new = dot(r, r, 3)
-        beta = rr_new / rr
-        p.mul_(beta.to(torch.float32)).add_(r)
-        rr.copy_(rr_new)
+        Ap = A(p).contiguous()
+        ops.dot(p, Ap, pAp)
+        ops.update_x(x, r, p, Ap, rr, pAp)
+        ops.dot(r, r, rr_new)
+        ops.update_p(p, r, rr, rr_new)
         k_dev.add_(1)
-        hist.index_copy_(0, k_dev.view(1), torch.sqrt(rr / bb).view(1))
+        hist.index_copy_(0, k_dev.view(1), torch.sqrt(rr / bb))
 
     if graph:
         # capture one iteration (after a warm-up on a side stream) and replay it

@@ -5,6 +5,10 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
 #include "tg_internal.cuh"
 
 namespace {
@@ -67,9 +71,11 @@ tg_status make_geometry(tg::Geometry &G, const tg_map_header *mh, const tg_image
     G.mh.mmin[k] = mh->mmin[k];
     G.mh.mmax[k] = mh->mmax[k];
     G.cdeltf[k] = (float)mh->cdelt[k];
+    G.cdeltl[k] = (float)(mh->cdelt[k] - (double)G.cdeltf[k]);
     G.mminf[k] = (float)mh->mmin[k];
     G.mmaxf[k] = (float)mh->mmax[k];
     G.inv_cdelt[k] = 1.0 / mh->cdelt[k];
+    G.inv_cdeltf[k] = (float)(1.0 / mh->cdelt[k]);
   }
   G.ms[3] = four_d ? ms[3] : 0;
   G.nframes = four_d ? (int)map_shape[3] : 1;
@@ -282,6 +288,109 @@ tg_status tg_segment_counts(const tg_map_header *map_header, const tg_image_head
     if (e != cudaSuccess) return launch_status(e, "segment count launch");
   }
   return TG_OK;
+}
+
+size_t tg_packed_plan_bytes(int32_t n_jobs) {
+  if (n_jobs < 0) return 0;
+  return tg::packed_records_offset(n_jobs) + (((size_t)n_jobs * tg::packed_job_bytes() + 255) & ~(size_t)255);
+}
+
+tg_status tg_packed_plan(const tg_job *jobs, int32_t n_jobs, int32_t rows_per_warp, int32_t four_d, void *plan,
+                         size_t plan_bytes, tg_packed_info *info) {
+  if (!info) return fail(TG_EINVAL, "info is NULL");
+  if (n_jobs <= 0 || !jobs) return fail(TG_EINVAL, "no jobs");
+  if (rows_per_warp != 1 && rows_per_warp != 2 && rows_per_warp != 4)
+    return fail(TG_EINVAL, "rows_per_warp must be 1, 2 or 4");
+  if (!plan || plan_bytes < tg_packed_plan_bytes(n_jobs)) return fail(TG_ENOMEM, "plan buffer too small");
+  const int rows = rows_per_warp * tg::kRows;
+  struct Item {
+    double work;
+    int idx;
+  };
+  std::vector<Item> order((size_t)n_jobs);
+  std::vector<tg::Geometry> geoms((size_t)n_jobs);
+  bool idx64 = false;
+  for (int j = 0; j < n_jobs; ++j) {
+    const tg_job &J = jobs[j];
+    bool i64 = false;
+    tg_status st = make_geometry(geoms[j], &J.map_header, J.views, J.n_views, J.n1, J.n2, J.data_strides,
+                                 J.map_shape, J.map_strides, J.mask, (tg_dtype)J.mask_dtype, J.mask_strides,
+                                 four_d != 0, &i64);
+    if (st != TG_OK) return fail(st, "job %d: %s", j, g_err);
+    if (J.n_views > 0 && J.n1 > 0 && J.n2 > 0 && (!J.data || !J.map))
+      return fail(TG_EINVAL, "job %d: data or map pointer is NULL", j);
+    idx64 = idx64 || i64;
+    order[j] = {(double)J.n_views * J.n1 * J.n2 * (double)(J.map_shape[0] + J.map_shape[1] + J.map_shape[2]), j};
+  }
+  std::stable_sort(order.begin(), order.end(), [](const Item &a, const Item &b) { return a.work > b.work; });
+  std::vector<unsigned char> host(tg_packed_plan_bytes(n_jobs), 0);
+  const size_t rec0 = tg::packed_records_offset(n_jobs);
+  long long tiles = 0;
+  for (int k = 0; k < n_jobs; ++k) {
+    const int j = order[k].idx;
+    const tg_job &J = jobs[j];
+    const int gx = (int)((J.n2 + 31) / 32), gy = (int)((J.n1 + rows - 1) / rows);
+    std::memcpy(host.data() + (size_t)k * sizeof(long long), &tiles, sizeof(long long));
+    tg::packed_fill(host.data() + rec0 + (size_t)k * tg::packed_job_bytes(), geoms[j], J.data, J.map, tiles, gx, gy);
+    tiles += (long long)gx * gy * J.n_views;
+  }
+  if (tiles > 2147483647LL) return fail(TG_EUNSUPPORTED, "packed launch of %lld CTAs is too large", tiles);
+  cudaError_t e = cudaMemcpy(plan, host.data(), host.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return launch_status(e, "plan upload");
+  info->n_jobs = n_jobs;
+  info->rows_per_warp = rows_per_warp;
+  info->four_d = four_d != 0;
+  info->idx64 = idx64 ? 1 : 0;
+  info->tiles = tiles;
+  return TG_OK;
+}
+
+tg_status tg_packed_projector(const void *plan, const tg_packed_info *info, int32_t mode, int32_t obstacle,
+                              void *stream) {
+  if (!plan || !info) return fail(TG_EINVAL, "NULL plan");
+  if (obstacle != TG_OBSTACLE_NONE && obstacle != TG_OBSTACLE_SUN)
+    return fail(TG_EINVAL, "obstacle must be none or sun");
+  const bool four_d = (mode == TG_PJT || mode == TG_BPJT);
+  if (mode < TG_PJ || mode > TG_BPJT || four_d != (info->four_d != 0))
+    return fail(TG_EINVAL, "mode does not match the plan (3-D / 4-D)");
+  if (info->tiles <= 0) return TG_OK;
+  return launch_status(tg::launch_packed(plan, info->n_jobs, info->tiles, info->rows_per_warp, info->idx64 != 0,
+                                         mode, obstacle, (cudaStream_t)stream),
+                       "packed projector launch");
+}
+
+size_t tg_segmented_workspace_bytes(int32_t n_seg) { return n_seg > 0 ? tg::seg_workspace_bytes(n_seg) : 0; }
+
+tg_status tg_segmented_dot_f32(const float *a, const float *b, const int64_t *off, int32_t n_seg, double *out,
+                               void *workspace, size_t workspace_bytes, void *stream) {
+  if (!a || !b || !off || !out || n_seg <= 0 || n_seg > 65535) return fail(TG_EINVAL, "bad segmented dot arguments");
+  if (!workspace || workspace_bytes < tg::seg_workspace_bytes(n_seg))
+    return fail(TG_ENOMEM, "segmented dot workspace needs %zu bytes", tg::seg_workspace_bytes(n_seg));
+  return launch_status(tg::launch_seg_dot(a, b, (const long long *)off, n_seg, (double *)workspace, out,
+                                          (cudaStream_t)stream),
+                       "segmented dot launch");
+}
+
+tg_status tg_cg_update_x(float *x, float *r, const float *p, const float *Ap, const double *rr, const double *pAp,
+                         const int64_t *off, int32_t n_seg, void *stream) {
+  if (!x || !r || !p || !Ap || !rr || !pAp || !off || n_seg <= 0 || n_seg > 65535)
+    return fail(TG_EINVAL, "bad CG update arguments");
+  return launch_status(
+      tg::launch_seg_cg_x(x, r, p, Ap, rr, pAp, (const long long *)off, n_seg, (cudaStream_t)stream), "CG update");
+}
+
+tg_status tg_cg_update_p(float *p, const float *r, double *rr, const double *rr_new, const int64_t *off,
+                         int32_t n_seg, void *stream) {
+  if (!p || !r || !rr || !rr_new || !off || n_seg <= 0 || n_seg > 65535) return fail(TG_EINVAL, "bad CG update arguments");
+  return launch_status(tg::launch_seg_cg_p(p, r, rr, rr_new, (const long long *)off, n_seg, (cudaStream_t)stream),
+                       "CG update");
+}
+
+tg_status tg_segmented_axpby(float *y, const float *x, float alpha, float beta, const int64_t *seg, int32_t n_seg,
+                             void *stream) {
+  if (!y || !seg || n_seg <= 0 || n_seg > 65535) return fail(TG_EINVAL, "bad segmented axpby arguments");
+  return launch_status(tg::launch_seg_axpby(y, x, alpha, beta, (const long long *)seg, n_seg, (cudaStream_t)stream),
+                       "segmented axpby");
 }
 
 size_t tg_noalloc_scratch_bytes(void) { return tg::noalloc_scratch_bytes(); }

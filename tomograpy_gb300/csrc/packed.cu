@@ -1,0 +1,226 @@
+// Packed multi-job launches: many independent reconstructions (each with its
+// own cube size, view count, image size and geometry) traced by ONE kernel
+// launch, and the per-job (segmented) vector kernels of a batched CG.
+//
+// A plan is a device buffer holding the first CTA tile of every job (int64,
+// ascending) followed by one PackedJob record per job (the job's kernel
+// Geometry and its data / cube pointers), sorted by decreasing work.  A CTA
+// finds its job by binary search on the compact tile array, copies the job's
+// record into shared memory and runs the same tile body as the single-job
+// kernel.
+#include "siddon_fast.cuh"
+
+namespace tg {
+
+struct PackedJob {
+  Geometry G;
+  float *data;
+  float *cube;
+  long long tile0;  // first CTA tile of this job
+  int gx, gy;       // column / row tiles per view
+};
+
+template <int MODE, bool SUN, typename IDX, int RPW>
+__global__ void __launch_bounds__(kThreads, min_blocks(MODE))
+    packed_kernel(const long long *__restrict__ tile0, const PackedJob *__restrict__ jobs, int n_jobs) {
+  static_assert(sizeof(PackedJob) % 4 == 0, "job record copied as 32-bit words");
+  __shared__ int s_job;
+  __shared__ __align__(16) int s_rec[sizeof(PackedJob) / 4];
+  if (threadIdx.x == 0) {
+    const long long b = blockIdx.x;
+    int lo = 0, hi = n_jobs - 1;
+    while (lo < hi) {  // last job whose first tile is <= b
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(tile0 + mid) <= b) lo = mid;
+      else hi = mid - 1;
+    }
+    s_job = lo;
+  }
+  __syncthreads();
+  const int *src = reinterpret_cast<const int *>(jobs + s_job);
+  for (int k = threadIdx.x; k < (int)(sizeof(PackedJob) / 4); k += blockDim.x) s_rec[k] = __ldg(src + k);
+  __syncthreads();
+  const PackedJob &J = *reinterpret_cast<const PackedJob *>(s_rec);
+  long long local = (long long)blockIdx.x - J.tile0;
+  const int bx = (int)(local % J.gx);
+  local /= J.gx;
+  const int by = (int)(local % J.gy);
+  const int t = (int)(local / J.gy);
+  constexpr bool PJ = (MODE == TG_PJ || MODE == TG_PJT);
+  tile_body<MODE, SUN, IDX, false, RPW>(J.G, t, bx * 32, by * (RPW * kRows), PJ ? J.cube : J.data,
+                                        PJ ? J.data : J.cube, nullptr, nullptr);
+}
+
+template <int MODE, typename IDX, int RPW>
+static void launch_packed_rpw(const long long *tile0, const PackedJob *jobs, int n_jobs, long long tiles, bool sun,
+                              cudaStream_t s) {
+  if (sun) packed_kernel<MODE, true, IDX, RPW><<<(unsigned)tiles, kThreads, 0, s>>>(tile0, jobs, n_jobs);
+  else packed_kernel<MODE, false, IDX, RPW><<<(unsigned)tiles, kThreads, 0, s>>>(tile0, jobs, n_jobs);
+}
+
+template <int MODE, typename IDX>
+static void launch_packed_mode(const long long *tile0, const PackedJob *jobs, int n_jobs, long long tiles, int rpw,
+                               bool sun, cudaStream_t s) {
+  if (rpw == 1) launch_packed_rpw<MODE, IDX, 1>(tile0, jobs, n_jobs, tiles, sun, s);
+  else if (rpw == 2) launch_packed_rpw<MODE, IDX, 2>(tile0, jobs, n_jobs, tiles, sun, s);
+  else launch_packed_rpw<MODE, IDX, 4>(tile0, jobs, n_jobs, tiles, sun, s);
+}
+
+// byte offset of the job records in a plan of n_jobs jobs
+size_t packed_records_offset(int n_jobs) { return ((size_t)n_jobs * sizeof(long long) + 255) & ~(size_t)255; }
+
+cudaError_t launch_packed(const void *plan, int n_jobs, long long tiles, int rpw, bool idx64, int mode, int obstacle,
+                          cudaStream_t s) {
+  const long long *tile0 = (const long long *)plan;
+  const PackedJob *jobs = (const PackedJob *)((const unsigned char *)plan + packed_records_offset(n_jobs));
+  const bool sun = obstacle == TG_OBSTACLE_SUN;
+  if (idx64) {
+    switch (mode) {
+    case TG_PJ: launch_packed_mode<TG_PJ, long long>(tile0, jobs, n_jobs, tiles, rpw, sun, s); break;
+    case TG_BPJ: launch_packed_mode<TG_BPJ, long long>(tile0, jobs, n_jobs, tiles, rpw, sun, s); break;
+    case TG_PJT: launch_packed_mode<TG_PJT, long long>(tile0, jobs, n_jobs, tiles, rpw, sun, s); break;
+    default: launch_packed_mode<TG_BPJT, long long>(tile0, jobs, n_jobs, tiles, rpw, sun, s); break;
+    }
+  } else {
+    switch (mode) {
+    case TG_PJ: launch_packed_mode<TG_PJ, int>(tile0, jobs, n_jobs, tiles, rpw, sun, s); break;
+    case TG_BPJ: launch_packed_mode<TG_BPJ, int>(tile0, jobs, n_jobs, tiles, rpw, sun, s); break;
+    case TG_PJT: launch_packed_mode<TG_PJT, int>(tile0, jobs, n_jobs, tiles, rpw, sun, s); break;
+    default: launch_packed_mode<TG_BPJT, int>(tile0, jobs, n_jobs, tiles, rpw, sun, s); break;
+    }
+  }
+  return cudaGetLastError();
+}
+
+size_t packed_job_bytes() { return sizeof(PackedJob); }
+
+void packed_fill(void *dst, const Geometry &G, float *data, float *cube, long long tile0, int gx, int gy) {
+  PackedJob *J = (PackedJob *)dst;
+  J->G = G;
+  J->data = data;
+  J->cube = cube;
+  J->tile0 = tile0;
+  J->gx = gx;
+  J->gy = gy;
+}
+
+// ---------------------------------------------------------------------------
+// segmented vector kernels of the batched CG: segment s = [seg[2s], seg[2s+1])
+
+constexpr int kSegBlocks = 32;  // blocks per segment
+constexpr int kSegThreads = 256;
+
+__device__ __forceinline__ double seg_block_sum(double v) {
+  __shared__ double sh[kSegThreads / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) sh[warp] = v;
+  __syncthreads();
+  v = (threadIdx.x < kSegThreads / 32) ? sh[threadIdx.x] : 0.0;
+  if (warp == 0) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  }
+  return v;
+}
+
+// partial[s * kSegBlocks + b] = block b's share of <a, b>_s (float64)
+__global__ void __launch_bounds__(kSegThreads) seg_dot_partial(const float *__restrict__ a,
+                                                               const float *__restrict__ b,
+                                                               const long long *__restrict__ off,
+                                                               double *__restrict__ partial) {
+  const int s = blockIdx.y;
+  const long long lo = off[2 * s], hi = off[2 * s + 1];
+  double acc = 0.0;
+  for (long long i = lo + (long long)blockIdx.x * blockDim.x + threadIdx.x; i < hi;
+       i += (long long)gridDim.x * blockDim.x)
+    acc += (double)a[i] * b[i];
+  acc = seg_block_sum(acc);
+  if (threadIdx.x == 0) partial[s * kSegBlocks + blockIdx.x] = acc;
+}
+
+// out[s] = sum of segment s's partials in block order (deterministic)
+__global__ void seg_dot_final(const double *__restrict__ partial, int n_seg, double *__restrict__ out) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n_seg) return;
+  double acc = 0.0;
+  for (int b = 0; b < kSegBlocks; ++b) acc += partial[s * kSegBlocks + b];
+  out[s] = acc;
+}
+
+// x += alpha_s p, r -= alpha_s Ap with alpha_s = rr_s / pAp_s
+__global__ void __launch_bounds__(kSegThreads) seg_cg_x(float *__restrict__ x, float *__restrict__ r,
+                                                        const float *__restrict__ p, const float *__restrict__ Ap,
+                                                        const double *__restrict__ rr,
+                                                        const double *__restrict__ pAp,
+                                                        const long long *__restrict__ off) {
+  const int s = blockIdx.y;
+  const double den = pAp[s];
+  const float alpha = (den != 0.0) ? (float)(rr[s] / den) : 0.f;
+  const long long lo = off[2 * s], hi = off[2 * s + 1];
+  for (long long i = lo + (long long)blockIdx.x * blockDim.x + threadIdx.x; i < hi;
+       i += (long long)gridDim.x * blockDim.x) {
+    x[i] = fmaf(alpha, p[i], x[i]);
+    r[i] = fmaf(-alpha, Ap[i], r[i]);
+  }
+}
+
+// p = r + beta_s p with beta_s = rr_new_s / rr_s
+__global__ void __launch_bounds__(kSegThreads) seg_cg_p(float *__restrict__ p, const float *__restrict__ r,
+                                                        const double *__restrict__ rr,
+                                                        const double *__restrict__ rr_new,
+                                                        const long long *__restrict__ off) {
+  const int s = blockIdx.y;
+  const double den = rr[s];
+  const float beta = (den != 0.0) ? (float)(rr_new[s] / den) : 0.f;
+  const long long lo = off[2 * s], hi = off[2 * s + 1];
+  for (long long i = lo + (long long)blockIdx.x * blockDim.x + threadIdx.x; i < hi;
+       i += (long long)gridDim.x * blockDim.x)
+    p[i] = fmaf(beta, p[i], r[i]);
+}
+
+// y[i] = alpha * x[i] + beta * y[i] over the segments (beta = 0: y = alpha x)
+__global__ void __launch_bounds__(kSegThreads) seg_axpby(float *__restrict__ y, const float *__restrict__ x, float alpha,
+                                                         float beta, const long long *__restrict__ off) {
+  const int s = blockIdx.y;
+  const long long lo = off[2 * s], hi = off[2 * s + 1];
+  for (long long i = lo + (long long)blockIdx.x * blockDim.x + threadIdx.x; i < hi;
+       i += (long long)gridDim.x * blockDim.x)
+    y[i] = (beta == 0.f) ? (x ? alpha * x[i] : 0.f) : fmaf(alpha, x ? x[i] : 0.f, beta * y[i]);
+}
+
+cudaError_t launch_seg_axpby(float *y, const float *x, float alpha, float beta, const long long *off, int n_seg,
+                             cudaStream_t st) {
+  seg_axpby<<<dim3(kSegBlocks, n_seg), kSegThreads, 0, st>>>(y, x, alpha, beta, off);
+  return cudaGetLastError();
+}
+
+__global__ void seg_copy(double *__restrict__ dst, const double *__restrict__ src, int n) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) dst[s] = src[s];
+}
+
+cudaError_t launch_seg_dot(const float *a, const float *b, const long long *off, int n_seg, double *partial,
+                           double *out, cudaStream_t st) {
+  seg_dot_partial<<<dim3(kSegBlocks, n_seg), kSegThreads, 0, st>>>(a, b, off, partial);
+  seg_dot_final<<<(n_seg + 127) / 128, 128, 0, st>>>(partial, n_seg, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_seg_cg_x(float *x, float *r, const float *p, const float *Ap, const double *rr, const double *pAp,
+                            const long long *off, int n_seg, cudaStream_t st) {
+  seg_cg_x<<<dim3(kSegBlocks, n_seg), kSegThreads, 0, st>>>(x, r, p, Ap, rr, pAp, off);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_seg_cg_p(float *p, const float *r, double *rr, const double *rr_new, const long long *off,
+                            int n_seg, cudaStream_t st) {
+  seg_cg_p<<<dim3(kSegBlocks, n_seg), kSegThreads, 0, st>>>(p, r, rr, rr_new, off);
+  seg_copy<<<(n_seg + 127) / 128, 128, 0, st>>>(rr, rr_new, n_seg);
+  return cudaGetLastError();
+}
+
+size_t seg_workspace_bytes(int n_seg) { return (size_t)n_seg * kSegBlocks * sizeof(double); }
+
+}  // namespace tg

@@ -126,3 +126,30 @@ def empty_data(view_hdrs, dtype=np.float32):
     h0 = view_hdrs[0]
     return InfoArray(shape=(int(h0["NAXIS1"]), int(h0["NAXIS2"]), len(view_hdrs)), header=view_hdrs,
                      dtype=dtype)
+
+
+# Uneven multi-instance batch: seeded cube edges, view counts, image sides and
+# observer distances (the configuration of the packed-launch benchmark).
+UNEVEN_EDGES = (32, 48, 64, 96, 128, 160, 192)
+UNEVEN_SIDES = (64, 128, 256, 512)
+
+
+def uneven_specs(n_jobs=32, seed=0, edges=UNEVEN_EDGES, sides=UNEVEN_SIDES, views=(16, 256), dist=(150.0, 230.0)):
+    """List of dicts {n, T, N, d, lon_range} for ``n_jobs`` seeded jobs."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n_jobs):
+        out.append(dict(n=int(rng.choice(edges)), T=int(rng.integers(views[0], views[1] + 1)),
+                        N=int(rng.choice(sides)), d=float(rng.uniform(*dist)),
+                        lon_range=(0.0, float(rng.uniform(np.pi, 2 * np.pi)))))
+    return out
+
+
+def make_job(spec, seed=0, with_data=True):
+    """(cube header, view headers, phantom, noisy data) for one job spec."""
+    from .batch import Job
+    ch, vh = make_geometry(spec)
+    job = Job(ch, vh)
+    if with_data:
+        job.phantom = phantom(ch, seed=seed) / np.float32(1e8)
+    return job

@@ -37,7 +37,7 @@ if ROOT not in sys.path:
 
 METRIC = "proj+backproj rays/s"
 UNIT = "rays/s"
-WORKLOAD = "cfg1"
+WORKLOAD = "recon256"
 WORKLOAD_DESC = ("differentiable-reconstruction geometry: 256^3 f32 cube on [-1.5,1.5] Rsun, 360 views of "
                  "512x512 over 0-360 deg at d=215 Rsun, obstacle=sun; step = projection + backprojection")
 L2_FLUSH_BYTES = 256 << 20
@@ -52,6 +52,10 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the uneven multi-job batch measurement")
+    ap.add_argument("--no-served", action="store_true", help="skip the serving-stream measurement")
+    ap.add_argument("--served-jobs", type=int, default=60,
+                    help="requests of the serving stream sample (Poisson, 20 jobs/s)")
     ap.add_argument("--profile-case", action="store_true",
                     help="one projection + one backprojection on the workload's geometry restricted to every "
                          "10th view (36 views): the case the ncu summaries in profiles/ are captured on")
@@ -127,13 +131,13 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def ncu_traffic():
-    """DRAM bytes per launch of the dominant kernel from the committed ncu
-    summary (profiles/siddon_bpj_f32_cfg1.md), scaled to the full workload."""
-    path = os.path.join(ROOT, "profiles", "siddon_bpj_f32_cfg1.md")
+def ncu_traffic(kernel):
+    """DRAM bytes (read + write) per launch of ``kernel`` on the full workload,
+    from the committed ncu summary profiles/siddon_f32_dram_256cube_360x512.md."""
+    path = os.path.join(ROOT, "profiles", "siddon_f32_dram_256cube_360x512.md")
     try:
         for line in open(path):
-            if line.startswith("dram_bytes_per_launch_full_workload:"):
+            if line.startswith(kernel + " dram_bytes_per_launch:"):
                 return float(line.split(":")[1].split()[0])
     except Exception:
         pass
@@ -300,7 +304,7 @@ def run_ours(args):
         k["gbs"] = k["bytes"] / (k["ms"] / 1000.0) / 1e9
         k["frac"] = k["gbs"] / peak
     dom = max(kern, key=lambda k: kern[k]["ms"])
-    traffic = ncu_traffic() if dom == "siddon_bpj_f32" else None
+    traffic = ncu_traffic(dom)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": kern[dom]["gbs"], "peak": peak, "unit": "GB/s",
                 "frac": kern[dom]["frac"], "traffic": traffic, "peak_kind": peak_kind + " hbm_gbs",
                 "algorithmic_bytes_per_launch": kern[dom]["bytes"]}
@@ -328,6 +332,12 @@ def run_ours(args):
                "h2d_bytes_per_step": vol + img, "d2h_bytes_per_step": img + vol,
                "path": "lo_wrapper.siddon_lo project/backproject, pinned host tensors"}
 
+    batched = served = None
+    if rank == 0 and not args.no_batched:
+        batched = measure_batched(dev)
+    if rank == 0 and not args.no_served:
+        served = measure_served(dev, args.served_jobs)
+
     if rank == 0:
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -343,10 +353,77 @@ def run_ours(args):
             "e2e": e2e,
             "gpu_launches": 2 * args.steps,
             "clocks": clk,
+            "batched": batched,
+            "served": served,
         }
         print(json.dumps(out), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def measure_batched(dev, n_jobs=32, iters=20, seed=0):
+    """Uneven multi-job batch: 32 seeded reconstructions (cube edge in
+    {32..192}, 16-256 views of 64-512 px, d in [150, 230]), 20 CG iterations
+    on (P^T P + 1e-2 I) x = P^T y each, solved (a) together with one packed
+    launch per direction per iteration, CUDA-graph captured, tile shape
+    autotuned, and (b) one after another with the single-job operator."""
+    import torch
+
+    from tomograpy_gb300 import batch, synthetic
+    specs = synthetic.uneven_specs(n_jobs, seed=seed)
+    jobs = [synthetic.make_job(s, seed=k) for k, s in enumerate(specs)]
+    pack = batch.PackedJobs(jobs, obstacle="sun", device=dev)
+    x = pack.new_cube()
+    for k, j in enumerate(jobs):
+        pack.cube_view(x, k).copy_(torch.from_numpy(j.phantom))
+    pack.project(x)
+    b = pack.backproject(pack.new_cube())
+    rhs = [pack.cube_view(b, k).clone() for k in range(n_jobs)]
+    batch.batched_cg(pack, b, iters=2)          # warm-up (graph capture path)
+    batch.sequential_cg(jobs[:2], rhs[:2], iters=2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    xb, _ = batch.batched_cg(pack, b, iters=iters)
+    torch.cuda.synchronize()
+    tb = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    xs = batch.sequential_cg(jobs, rhs, iters=iters)
+    torch.cuda.synchronize()
+    ts = time.perf_counter() - t0
+    diff = max(float((pack.cube_view(xb, k) - xs[k]).abs().max() / xs[k].abs().max().clamp_min(1e-30))
+               for k in range(n_jobs))
+    rays = sum(int(j.data_shape[0] * j.data_shape[1] * j.data_shape[2]) for j in jobs)
+    return {"workload": "uneven batch: %d seeded jobs (edges 32-192, 16-256 views, 64-512 px), %d CG iterations, "
+                        "sun" % (n_jobs, iters),
+            "rays_per_iteration": rays, "rows_per_warp": pack.rows_per_warp,
+            "batched_cg_it_per_s": n_jobs * iters / tb, "plain_cg_it_per_s": n_jobs * iters / ts,
+            "speedup": ts / tb, "batched_s": tb, "plain_s": ts, "max_rel_diff_vs_plain": diff,
+            "plain": "one job after another: single-job operator + the same CG kernels (no graph)"}
+
+
+def measure_served(dev, n_jobs=60, rate=20.0, seed=0):
+    """Serving stream sample: Poisson arrivals (20 jobs/s, seeded), sizes as the
+    uneven batch plus 10 % large jobs (256^3, 360 x 512^2), 20 CG iterations
+    or relative residual 1e-4 each; continuous batching vs a FIFO plain loop."""
+    import numpy as np
+
+    from tomograpy_gb300 import serve, synthetic
+    rng = np.random.default_rng(seed + 99)
+    specs = synthetic.uneven_specs(n_jobs, seed=seed + 1)
+    for k in range(n_jobs):
+        if rng.random() < 0.1:
+            specs[k] = dict(synthetic.CONFIGS["recon256"])
+    reqs = serve.poisson_requests(specs, rate=rate, seed=seed, max_iters=20, tol=1e-4, device=dev)
+    srv = serve.Server(device=dev)
+    s = srv.run(reqs)
+    reqs2 = serve.poisson_requests(specs, rate=rate, seed=seed, max_iters=20, tol=1e-4, device=dev)
+    f = serve.fifo_plain(reqs2, device=dev)
+    diff = max(float((a.result - c.result).abs().max() / c.result.abs().max().clamp_min(1e-30))
+               for a, c in zip(reqs, reqs2))
+    return {"workload": "serving stream: %d Poisson requests at %.0f jobs/s, uneven sizes + 10%% 256^3 x 360 x "
+                        "512^2, 20 CG iterations or residual 1e-4" % (n_jobs, rate),
+            "served": s, "fifo_plain": f, "cg_it_per_s_ratio": s["cg_it_per_s"] / f["cg_it_per_s"],
+            "max_inflight": srv.max_inflight, "max_rel_diff_vs_plain": diff}
 
 
 def run_profile_case():

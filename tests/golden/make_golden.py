@@ -12,12 +12,12 @@ files to pin the oracle (``tests/test_oracle_golden.py``) and the CUDA path
 
 Cases (all float64 unless stated):
 
-* ``cfg0s``  -- the plain-method geometry at reduced size: 24^3 cube spanning
+* ``small24``  -- the plain-method geometry at reduced size: 24^3 cube spanning
   [-1.5, 1.5], 13 views of 40^2 over 0..pi (so lon = 0 and lon = pi, the
   degenerate views, are included), d = 215, shell + blob phantom; pj / bpj
   with obstacle sun and none, with and without a data mask, plus the
   reference's float32 path for pj (to record its own float32 error);
-* ``cfg0s4`` -- pjt / bpjt on a 12^3 x 7-frame cube, 7 views of 24^2;
+* ``frames12`` -- pjt / bpjt on a 12^3 x 7-frame cube, 7 views of 24^2;
 * ``cases`` -- the reference test-suite geometry (``tests/test_cases.py``): a
   16^3 and a 1^3 cube spanning 3 radii, 32^2 images whose field of view is
   ``fov(obj, 200)``, 17 views over 0..2 pi at radius 200; projection of ones,
@@ -59,7 +59,7 @@ def ref_run(data, cube, mask, obstacle, mode, ctype="double"):
     mod.conic_full_projector(data, cube, mask, 1)
 
 
-def cfg0s(out):
+def small24(out):
     n, T, N, d = 24, 13, 40, 215.0
     ch = synthetic.cube_header(n, dtype=np.float64)
     vh = synthetic.view_headers(T, N, d=d, lon_range=(0.0, np.pi), dtype=np.float64)
@@ -67,11 +67,11 @@ def cfg0s(out):
     rng = np.random.default_rng(11)
     y = rng.random((N, N, T))
     mask = (rng.random((N, N, T)) < 0.1).astype(np.float64)
-    out["cfg0s_views"] = pack_views(vh)
-    out["cfg0s_cube_hdr"] = pack_cube(ch)
-    out["cfg0s_x"] = x
-    out["cfg0s_y"] = y
-    out["cfg0s_mask"] = mask
+    out["small24_views"] = pack_views(vh)
+    out["small24_cube_hdr"] = pack_cube(ch)
+    out["small24_x"] = x
+    out["small24_y"] = y
+    out["small24_mask"] = mask
     for obstacle in ("sun", "none"):
         for use_mask in (False, True):
             m = mask if use_mask else np.zeros((N, N, T))
@@ -79,19 +79,19 @@ def cfg0s(out):
             data = InfoArray(data=np.zeros((N, N, T)), header=[dict(h) for h in vh])
             cube = InfoArray(data=x.copy(), header=dict(ch))
             ref_run(data, cube, m, obstacle, "pj")
-            out["cfg0s_pj_" + tag] = np.asarray(data)
+            out["small24_pj_" + tag] = np.asarray(data)
             data = InfoArray(data=y.copy(), header=[dict(h) for h in vh])
             cube = InfoArray(data=np.zeros((n, n, n)), header=dict(ch))
             ref_run(data, cube, m, obstacle, "bpj")
-            out["cfg0s_bpj_" + tag] = np.asarray(cube)
+            out["small24_bpj_" + tag] = np.asarray(cube)
     # the reference's own float32 path on the same inputs
     data = InfoArray(data=np.zeros((N, N, T), np.float32), header=[dict(h) for h in vh])
     cube = InfoArray(data=x.astype(np.float32), header=dict(ch))
     ref_run(data, cube, np.zeros((N, N, T), np.float32), "sun", "pj", ctype="float")
-    out["cfg0s_pj_sun_nomask_float32ref"] = np.asarray(data)
+    out["small24_pj_sun_nomask_float32ref"] = np.asarray(data)
 
 
-def cfg0s4(out):
+def frames12(out):
     """4-D variants on a smaller geometry: 12^3 x 7 frames, 7 views of 24^2."""
     n, T, N, d = 12, 7, 24, 215.0
     ch = synthetic.cube_header(n, dtype=np.float64)
@@ -99,19 +99,19 @@ def cfg0s4(out):
     x = synthetic.phantom(ch, seed=5, dtype=np.float64)
     x4 = np.stack([x * (1.0 + 0.1 * t) for t in range(T)], axis=-1)
     y = np.random.default_rng(12).random((N, N, T))
-    out["cfg0s4_views"] = pack_views(vh)
-    out["cfg0s4_cube_hdr"] = pack_cube(ch)
-    out["cfg0s4_x4"] = x4
-    out["cfg0s4_y"] = y
+    out["frames12_views"] = pack_views(vh)
+    out["frames12_cube_hdr"] = pack_cube(ch)
+    out["frames12_x4"] = x4
+    out["frames12_y"] = y
     for obstacle in ("sun", "none"):
         data = InfoArray(data=np.zeros((N, N, T)), header=[dict(h) for h in vh])
         cube = InfoArray(data=x4.copy(), header=dict(ch))
         ref_run(data, cube, np.zeros((N, N, T)), obstacle, "pjt")
-        out["cfg0s4_pjt_" + obstacle] = np.asarray(data)
+        out["frames12_pjt_" + obstacle] = np.asarray(data)
         data = InfoArray(data=y.copy(), header=[dict(h) for h in vh])
         cube = InfoArray(data=np.zeros((n, n, n, T)), header=dict(ch))
         ref_run(data, cube, np.zeros((N, N, T)), obstacle, "bpjt")
-        out["cfg0s4_bpjt_" + obstacle] = np.asarray(cube)
+        out["frames12_bpjt_" + obstacle] = np.asarray(cube)
 
 
 def test_case_geometry(n_cube, n_images, n_pix=32):
@@ -161,8 +161,8 @@ def diag(out):
 def main():
     build_ref.build(quiet=True)
     out = {}
-    cfg0s(out)
-    cfg0s4(out)
+    small24(out)
+    frames12(out)
     cases(out)
     diag(out)
     path = os.path.join(HERE, "reference_siddon.npz")

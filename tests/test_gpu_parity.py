@@ -32,18 +32,18 @@ def _hdrs(vh):
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
 def test_golden_projection(obstacle, use_mask, dtype):
     g = golden()
-    vh, ch = golden_case("cfg0s", 40, 40, (24, 24, 24))
+    vh, ch = golden_case("small24", 40, 40, (24, 24, 24))
     degen = degenerate_rays(vh, 40, 40)
     assert degen.any()  # the lon = pi view is in this geometry
     data = InfoArray(shape=(40, 40, 13), header=_hdrs(vh), dtype=dtype)
-    cube = InfoArray(data=g["cfg0s_x"].astype(dtype), header=dict(ch))
-    mask = g["cfg0s_mask"] if use_mask else None
+    cube = InfoArray(data=g["small24_x"].astype(dtype), header=dict(ch))
+    mask = g["small24_mask"] if use_mask else None
     tg.projector(data, cube, mask=mask, obstacle=obstacle)
-    ref = g["cfg0s_pj_%s_%s" % (obstacle, "mask" if use_mask else "nomask")]
+    ref = g["small24_pj_%s_%s" % (obstacle, "mask" if use_mask else "nomask")]
     if dtype == np.float32:
         # the reference's float64 output on the float32-rounded cube is the target
         r = InfoArray(shape=(40, 40, 13), header=_hdrs(vh))
-        oracle.projector(r, InfoArray(data=g["cfg0s_x"].astype(np.float32).astype(np.float64), header=dict(ch)),
+        oracle.projector(r, InfoArray(data=g["small24_x"].astype(np.float32).astype(np.float64), header=dict(ch)),
                          mask=mask, obstacle=obstacle)
         rel, norm = image_errors(data, r, exclude=degen)
         assert rel <= IMG_TOL and norm <= IMG_TOL, (rel, norm)
@@ -58,9 +58,9 @@ def test_golden_projection(obstacle, use_mask, dtype):
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
 def test_golden_backprojection(obstacle, dtype):
     g = golden()
-    vh, ch = golden_case("cfg0s", 40, 40, (24, 24, 24))
+    vh, ch = golden_case("small24", 40, 40, (24, 24, 24))
     degen = degenerate_rays(vh, 40, 40)
-    y = g["cfg0s_y"].copy()
+    y = g["small24_y"].copy()
     y[degen] = 0.0  # degenerate rays are compared separately
     cube = InfoArray(shape=(24, 24, 24), header=dict(ch), dtype=dtype)
     tg.backprojector(InfoArray(data=y.astype(dtype), header=_hdrs(vh)), cube, obstacle=obstacle)
@@ -102,7 +102,7 @@ def test_degenerate_rays_trace_their_chord():
     reference's double path returns rounding noise there (its plane distance
     next*p + a1 - amin cancels catastrophically, giving 0 or negative segment
     lengths), so those rays are checked against the exact chord instead."""
-    vh, ch = golden_case("cfg0s", 40, 40, (24, 24, 24))
+    vh, ch = golden_case("small24", 40, 40, (24, 24, 24))
     degen = degenerate_rays(vh, 40, 40)
     data = InfoArray(shape=(40, 40, 13), header=_hdrs(vh), dtype=np.float32)
     tg.projector(data, InfoArray(data=np.ones((24, 24, 24), np.float32), header=dict(ch)))
@@ -116,15 +116,15 @@ def test_degenerate_rays_trace_their_chord():
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
 def test_golden_time_dependent(obstacle, dtype):
     g = golden()
-    vh, ch = golden_case("cfg0s4", 24, 24, (12, 12, 12, 7))
+    vh, ch = golden_case("frames12", 24, 24, (12, 12, 12, 7))
     degen = degenerate_rays(vh, 24, 24)
     data = InfoArray(shape=(24, 24, 7), header=_hdrs(vh), dtype=dtype)
-    cube = InfoArray(data=g["cfg0s4_x4"].astype(dtype), header=dict(ch))
+    cube = InfoArray(data=g["frames12_x4"].astype(dtype), header=dict(ch))
     tg.projector4d(data, cube, obstacle=obstacle)
-    rel, norm = image_errors(data, g["cfg0s4_pjt_" + obstacle], exclude=degen)
+    rel, norm = image_errors(data, g["frames12_pjt_" + obstacle], exclude=degen)
     tol = 2e-6 if dtype == np.float32 else 1e-12  # includes the float32 rounding of the cube
     assert norm <= tol, (rel, norm)
-    y = g["cfg0s4_y"].copy()
+    y = g["frames12_y"].copy()
     y[degen] = 0
     cube = InfoArray(shape=(12, 12, 12, 7), header=dict(ch), dtype=dtype)
     tg.backprojector4d(InfoArray(data=y.astype(dtype), header=_hdrs(vh)), cube, obstacle=obstacle)
@@ -274,8 +274,8 @@ def _compare_pj_bpj(ch, vh, x, y, obstacle, shape_img):
 
 
 @pytest.mark.parametrize("obstacle", ["sun", None])
-def test_cfg0_full_size_phantom(obstacle):
-    ch, vh = synthetic.make_geometry("cfg0")
+def test_plain64_full_size_phantom(obstacle):
+    ch, vh = synthetic.make_geometry("plain64")
     x = synthetic.phantom(ch, seed=0)
     y = np.random.default_rng(1).random((128, 128, 60))
     _compare_pj_bpj(ch, vh, x, y, obstacle, (128, 128, 60))
@@ -317,7 +317,7 @@ def test_observer_inside_cube_and_small_cube_inside_sun():
 
 
 def test_adjoint_dot_product():
-    ch, vh = synthetic.make_geometry("cfg0")
+    ch, vh = synthetic.make_geometry("plain64")
     rng = np.random.default_rng(5)
     x = rng.random((64, 64, 64)).astype(np.float32)
     y = rng.random((128, 128, 60)).astype(np.float32)

@@ -88,7 +88,7 @@ def test_intersect_cube_matches_reference_nonzero_pattern():
 
 
 def test_synthetic_geometry():
-    ch, vh = synthetic.make_geometry("cfg0")
+    ch, vh = synthetic.make_geometry("plain64")
     assert ch["NAXIS1"] == 64 and len(vh) == 60 and vh[0]["NAXIS1"] == 128
     fov = vh[0]["CDELT1"] * 128 / 2
     assert np.isclose(np.tan(fov) * 215.0, 1.6)

@@ -30,49 +30,49 @@ def _build(built):
 
 @pytest.mark.parametrize("obstacle", ["sun", "none"])
 @pytest.mark.parametrize("use_mask", [False, True])
-def test_cfg0s_projection(obstacle, use_mask):
+def test_small24_projection(obstacle, use_mask):
     g = golden()
-    vh, ch = golden_case("cfg0s", 40, 40, (24, 24, 24))
+    vh, ch = golden_case("small24", 40, 40, (24, 24, 24))
     data = InfoArray(shape=(40, 40, 13), header=vh)
-    cube = InfoArray(data=g["cfg0s_x"].copy(), header=ch)
-    oracle.projector(data, cube, mask=g["cfg0s_mask"] if use_mask else None, obstacle=obstacle)
+    cube = InfoArray(data=g["small24_x"].copy(), header=ch)
+    oracle.projector(data, cube, mask=g["small24_mask"] if use_mask else None, obstacle=obstacle)
     tag = "%s_%s" % (obstacle, "mask" if use_mask else "nomask")
-    _same(data, g["cfg0s_pj_" + tag], exact=X86)
+    _same(data, g["small24_pj_" + tag], exact=X86)
 
 
 @pytest.mark.parametrize("obstacle", ["sun", "none"])
 @pytest.mark.parametrize("use_mask", [False, True])
-def test_cfg0s_backprojection(obstacle, use_mask):
+def test_small24_backprojection(obstacle, use_mask):
     g = golden()
-    vh, ch = golden_case("cfg0s", 40, 40, (24, 24, 24))
-    data = InfoArray(data=g["cfg0s_y"].copy(), header=vh)
+    vh, ch = golden_case("small24", 40, 40, (24, 24, 24))
+    data = InfoArray(data=g["small24_y"].copy(), header=vh)
     cube = InfoArray(shape=(24, 24, 24), header=ch)
-    oracle.backprojector(data, cube, mask=g["cfg0s_mask"] if use_mask else None, obstacle=obstacle, nthread=1)
+    oracle.backprojector(data, cube, mask=g["small24_mask"] if use_mask else None, obstacle=obstacle, nthread=1)
     tag = "%s_%s" % (obstacle, "mask" if use_mask else "nomask")
-    _same(cube, g["cfg0s_bpj_" + tag], exact=X86)
+    _same(cube, g["small24_bpj_" + tag], exact=X86)
 
 
 @pytest.mark.parametrize("obstacle", ["sun", "none"])
-def test_cfg0s4_time_dependent(obstacle):
+def test_frames12_time_dependent(obstacle):
     g = golden()
-    vh, ch = golden_case("cfg0s4", 24, 24, (12, 12, 12, 7))
+    vh, ch = golden_case("frames12", 24, 24, (12, 12, 12, 7))
     data = InfoArray(shape=(24, 24, 7), header=vh)
-    cube = InfoArray(data=g["cfg0s4_x4"].copy(), header=ch)
+    cube = InfoArray(data=g["frames12_x4"].copy(), header=ch)
     oracle.projector4d(data, cube, obstacle=obstacle)
-    _same(data, g["cfg0s4_pjt_" + obstacle], exact=X86)
-    data = InfoArray(data=g["cfg0s4_y"].copy(), header=vh)
+    _same(data, g["frames12_pjt_" + obstacle], exact=X86)
+    data = InfoArray(data=g["frames12_y"].copy(), header=vh)
     cube = InfoArray(shape=(12, 12, 12, 7), header=ch)
     oracle.backprojector4d(data, cube, obstacle=obstacle, nthread=1)
-    _same(cube, g["cfg0s4_bpjt_" + obstacle], exact=X86)
+    _same(cube, g["frames12_bpjt_" + obstacle], exact=X86)
 
 
 def test_float32_path_matches_reference_float32():
     g = golden()
-    vh, ch = golden_case("cfg0s", 40, 40, (24, 24, 24))
+    vh, ch = golden_case("small24", 40, 40, (24, 24, 24))
     data = InfoArray(shape=(40, 40, 13), header=vh, dtype=np.float32)
-    cube = InfoArray(data=g["cfg0s_x"].astype(np.float32), header=ch)
+    cube = InfoArray(data=g["small24_x"].astype(np.float32), header=ch)
     oracle.projector(data, cube, obstacle="sun")
-    _same(data, g["cfg0s_pj_sun_nomask_float32ref"], exact=X86)
+    _same(data, g["small24_pj_sun_nomask_float32ref"], exact=X86)
 
 
 @pytest.mark.parametrize("n_cube", [16, 1])
@@ -104,10 +104,10 @@ def test_diagnostics():
 def test_golden_planted_error_is_caught():
     """A mistake planted in the oracle's output must fail the comparison."""
     g = golden()
-    vh, ch = golden_case("cfg0s", 40, 40, (24, 24, 24))
+    vh, ch = golden_case("small24", 40, 40, (24, 24, 24))
     data = InfoArray(shape=(40, 40, 13), header=vh)
-    oracle.projector(data, InfoArray(data=g["cfg0s_x"].copy(), header=ch), obstacle="sun")
+    oracle.projector(data, InfoArray(data=g["small24_x"].copy(), header=ch), obstacle="sun")
     bad = np.asarray(data).copy()
     bad[20, 20, 3] *= 1.0 + 1e-9
     with pytest.raises(AssertionError):
-        _same(bad, g["cfg0s_pj_sun_nomask"], exact=True)
+        _same(bad, g["small24_pj_sun_nomask"], exact=True)

@@ -107,11 +107,11 @@ def poisson_noise(y, peak_counts=1e4, seed=0):
 # Config sizes of the benchmark workloads.
 CONFIGS = {
     # plain method, CPU-runnable
-    "cfg0": dict(n=64, T=60, N=128, d=215.0, lon_range=(0.0, np.pi)),
+    "plain64": dict(n=64, T=60, N=128, d=215.0, lon_range=(0.0, np.pi)),
     # differentiable reconstruction (the throughput headline)
-    "cfg1": dict(n=256, T=360, N=512, d=215.0, lon_range=(0.0, 2 * np.pi)),
+    "recon256": dict(n=256, T=360, N=512, d=215.0, lon_range=(0.0, 2 * np.pi)),
     # time-dependent: 28 frames x 28 views
-    "cfg2": dict(n=128, T=784, N=256, d=215.0, lon_range=(0.0, 2 * np.pi), n_frames=28),
+    "frames128": dict(n=128, T=784, N=256, d=215.0, lon_range=(0.0, 2 * np.pi), n_frames=28),
 }
 
 

@@ -474,6 +474,18 @@ __device__ __forceinline__ float walk_step(Walk<IDX> &w, float &cur, IDX &seg_of
 // the cube is not read).
 constexpr int kModeCount = 4;
 
+// Fire-and-forget float add to global memory.  Written out because a pointer
+// that the compiler cannot prove global (e.g. one read from shared memory in
+// the packed kernel) turns atomicAdd into a generic atomic that returns its
+// old value and stalls the warp until it does.
+__device__ __forceinline__ void red_add_f32(float *p, float v) {
+  asm volatile("red.global.add.f32 [%0], %1;" ::"l"(__cvta_generic_to_global(p)), "f"(v) : "memory");
+}
+
+__device__ __forceinline__ void red_add_u64(unsigned long long *p, unsigned long long v) {
+  asm volatile("red.global.add.u64 [%0], %1;" ::"l"(__cvta_generic_to_global(p)), "l"(v) : "memory");
+}
+
 // Accumulate one segment (length L, voxel offset o) in the mode's way.
 template <int MODE, bool DET, typename IDX>
 __device__ __forceinline__ void accumulate(float L, IDX o, const float *cin, float *cout, unsigned long long *aout,
@@ -483,9 +495,9 @@ __device__ __forceinline__ void accumulate(float L, IDX o, const float *cin, flo
   } else if (MODE == TG_PJ || MODE == TG_PJT) {
     acc = fmaf(L, __ldg(cin + o), acc);
   } else if (DET) {
-    atomicAdd(aout + o, (unsigned long long)__float2ll_rn((L * yq) * qs));
+    red_add_u64(aout + o, (unsigned long long)__float2ll_rn((L * yq) * qs));
   } else {
-    atomicAdd(cout + o, L * yv);
+    red_add_f32(cout + o, L * yv);
   }
 }
 

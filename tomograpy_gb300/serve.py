@@ -84,12 +84,14 @@ class Server:
     x, r, p, Ap and the data stack of every in-flight job)."""
 
     def __init__(self, budget_bytes=None, lam=1e-2, obstacle="sun", rows_per_warp=4, device=None,
-                 cube_fraction=0.4):
+                 cube_fraction=0.4, max_rays=1 << 23, max_wait=1.0):
         self.L = B._bind(_lib.load())
         self.dev = device or S._device()
         self.lam = float(lam)
         self.obstacle = obstacle
         self.rpw = rows_per_warp
+        self.max_rays = int(max_rays)
+        self.max_wait = float(max_wait)
         if budget_bytes is None:  # half of the free device memory
             budget_bytes = torch.cuda.mem_get_info(self.dev)[0] // 2
         # the budget is split once into two arenas: the four cube vectors of
@@ -234,6 +236,29 @@ class Server:
             self.dirty = True
         return len(done)
 
+    def _rays_inflight(self):
+        return sum(int(np.prod(r.job.data_shape)) for r, *_ in self.inflight)
+
+    def _admit(self, queue, now):
+        """Admit queued requests: in arrival order while the in-flight rays stay
+        under ``max_rays`` (one step is then a few tens of waves of the GPU, so
+        a newcomer waits at most one such step) and memory allows; a request
+        that does not fit is skipped by later, smaller ones (backfill) unless
+        it has waited ``max_wait`` seconds, and it is always admitted into an
+        empty server."""
+        rays = self._rays_inflight()
+        k = 0
+        while k < len(queue):
+            req = queue[k]
+            need = int(np.prod(req.job.data_shape))
+            if (not self.inflight or rays + need <= self.max_rays) and self.try_admit(req):
+                queue.pop(k)
+                rays += need
+                continue
+            if k == 0 and now - req.arrival >= self.max_wait:
+                break  # the head has waited long enough: let the server drain for it
+            k += 1
+
     def run(self, requests):
         """Serve ``requests`` (sorted by arrival time, seconds from now)."""
         pending = list(requests)
@@ -243,8 +268,7 @@ class Server:
             now = time.perf_counter() - self.t_start
             while pending and pending[0].arrival <= now:
                 queue.append(pending.pop(0))
-            while queue and self.try_admit(queue[0]):
-                queue.pop(0)
+            self._admit(queue, now)
             if not self.inflight:
                 if queue:
                     raise RuntimeError("request %d does not fit the memory budget" % queue[0].id)

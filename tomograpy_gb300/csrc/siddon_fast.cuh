@@ -46,7 +46,7 @@ namespace tg {
 // the gather-bound projection prefers longer batches, the atomic-bound
 // backprojection more resident warps).
 #ifndef TG_PJ_BATCH
-#define TG_PJ_BATCH 8
+#define TG_PJ_BATCH 20
 #endif
 #ifndef TG_PJ_MIN_BLOCKS
 #define TG_PJ_MIN_BLOCKS 3
@@ -57,7 +57,12 @@ namespace tg {
 #ifndef TG_BPJ_MIN_BLOCKS
 #define TG_BPJ_MIN_BLOCKS 4
 #endif
+#ifndef TG_PJ_DRIFT
+#define TG_PJ_DRIFT 1
+#endif
 __host__ __device__ constexpr bool is_backprojection(int mode) { return mode == TG_BPJ || mode == TG_BPJT; }
+// running-sum crossings inside projection batches (drift_step)
+__host__ __device__ constexpr bool drift_batches(int mode) { return !is_backprojection(mode) && TG_PJ_DRIFT; }
 // steps per batch of independent gathers / atomics
 __host__ __device__ constexpr int batch_steps(int mode) { return is_backprojection(mode) ? TG_BPJ_BATCH : TG_PJ_BATCH; }
 // CTAs per SM the register budget must allow
@@ -470,6 +475,40 @@ __device__ __forceinline__ float walk_step(Walk<IDX> &w, float &cur, IDX &seg_of
   return L;
 }
 
+// Step of a drift batch (projection): like walk_step, but an advanced family's
+// next crossing becomes t + |p| (one add instead of the count update and the
+// FMA) and the counts are not kept; resync() recovers them and recomputes
+// every crossing exactly after the batch.  Within a batch of kBatch steps
+// the running sums drift by at most kBatch / 2 ulp of |t|.
+template <typename IDX>
+__device__ __forceinline__ float drift_step(Walk<IDX> &w, float &cur, IDX &seg_off) {
+  const float tm = min3f(w.t[0], w.t[1], w.t[2]);
+  const float L = tm - cur;
+  seg_off = w.off;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    if (w.t[k] == tm) {
+      w.t[k] += w.pa[k];
+      w.off += w.st[k];
+    }
+  }
+  cur = tm;
+  return L;
+}
+
+// Exact counts and crossings after a drift batch: the drifted crossing is
+// within a few ulp of fma(m, p, d), so m = rint((t - d) / p).
+template <typename IDX>
+__device__ __forceinline__ void resync(Walk<IDX> &w) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    if (w.pa[k] != __int_as_float(0x7f800000)) {
+      w.m[k] = rintf(__fdividef(w.t[k] - w.d[k], w.pa[k]));
+      w.t[k] = fmaf(w.m[k], w.pa[k], w.d[k]);
+    }
+  }
+}
+
 // Internal mode: count the steps each ray takes (written to xout as float;
 // the cube is not read).
 constexpr int kModeCount = 4;
@@ -556,17 +595,37 @@ __device__ __forceinline__ void trace_fast(const Geometry &G, const tg_image_hea
   // that bound is below tstop every step of the batch starts before tstop:
   // the batch is exactly kBatch iterations of the single-step loop below, with
   // no per-step test, and its kBatch cube gathers are issued together.
+  //
+  // Projection batches drift (drift_step): their first kBatch - 1 crossings
+  // are running sums.  Every sum that can be taken lies in [-h, h] (h = half
+  // chord), so each add is off by at most 2^-24 h and a drifted crossing by at
+  // most (kBatch - 1) 2^-24 h; the bound gets a margin of (kBatch + 1) 2^-23 h,
+  // more than twice that, so a drifted step still advances only families
+  // whose exact crossing is below the stop.  The counts are then recovered
+  // (resync) and the batch's last step is an exact one.
   constexpr int kBatch = batch_steps(MODE);
+  constexpr bool kDrift = drift_batches(MODE);
+  const float margin = kDrift ? (float)(kBatch + 1) * 1.1920929e-7f * (-w.t0) : 0.f;
   while (guard >= kBatch) {
     const float bnd = min3f(fmaf(w.m[0] + (float)(kBatch - 2), w.pa[0], w.d[0]),
                             fmaf(w.m[1] + (float)(kBatch - 2), w.pa[1], w.d[1]),
                             fmaf(w.m[2] + (float)(kBatch - 2), w.pa[2], w.d[2]));
-    if (!(bnd < tstop)) break;
+    if (!(bnd + margin < tstop)) break;
     guard -= kBatch;
     float L[kBatch];
     IDX o[kBatch];
+    if (kDrift) {
+      // the batch's last step is exact, so `cur` leaves the batch exact and
+      // the stop test after it compares exact values (a drifted crossing just
+      // below an exact exit would let the next step read outside the cube)
 #pragma unroll
-    for (int s = 0; s < kBatch; ++s) L[s] = walk_step(w, cur, o[s]);
+      for (int s = 0; s < kBatch - 1; ++s) L[s] = drift_step(w, cur, o[s]);
+      resync(w);
+      L[kBatch - 1] = walk_step(w, cur, o[kBatch - 1]);
+    } else {
+#pragma unroll
+      for (int s = 0; s < kBatch; ++s) L[s] = walk_step(w, cur, o[s]);
+    }
     if (CNT) {
       acc += (float)kBatch;
     } else if (PJ) {

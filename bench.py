@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the uneven multi-job batch measurement")
     ap.add_argument("--no-served", action="store_true", help="skip the serving-stream measurement")
+    ap.add_argument("--no-4d", action="store_true", help="skip the time-dependent (4-D) measurement")
     ap.add_argument("--served-jobs", type=int, default=60,
                     help="requests of the serving stream sample (Poisson, 20 jobs/s)")
     ap.add_argument("--profile-case", action="store_true",
@@ -332,7 +333,9 @@ def run_ours(args):
                "h2d_bytes_per_step": vol + img, "d2h_bytes_per_step": img + vol,
                "path": "lo_wrapper.siddon_lo project/backproject, pinned host tensors"}
 
-    batched = served = None
+    batched = served = four_d = None
+    if rank == 0 and not args.no_4d:
+        four_d = measure_4d(dev)
     if rank == 0 and not args.no_batched:
         batched = measure_batched(dev)
     if rank == 0 and not args.no_served:
@@ -353,12 +356,69 @@ def run_ours(args):
             "e2e": e2e,
             "gpu_launches": 2 * args.steps,
             "clocks": clk,
+            "four_d": four_d,
             "batched": batched,
             "served": served,
         }
         print(json.dumps(out), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def measure_4d(dev, reps=5, cg_iters=30):
+    """Time-dependent workload: 128^3 x 28-frame cube (frame-major), 784 views
+    of 256^2 over 0-360 deg, view v -> frame v // 28, sun; projection +
+    backprojection rays/s (L2 flushed between steps), and 30 CG iterations on
+    (P^T P + 1e-2 I + 1e-2 D_t^T D_t) x = P^T y through the 4-D operator."""
+    import numpy as np
+    import torch
+
+    from tomograpy_gb300 import cg, lo_wrapper, siddon, synthetic
+    cfg = synthetic.CONFIGS["frames128"]
+    n, T, N, F = cfg["n"], cfg["T"], cfg["N"], cfg["n_frames"]
+    ch, vh = synthetic.make_geometry("frames128")
+    frames = np.arange(T) // (T // F)
+    views = siddon.upload_views(vh, frames, dev)
+    mh = siddon.pack_map_header(ch)
+    x4 = synthetic.phantom4d(ch, F, seed=0)                       # (n, n, n, F)
+    x = torch.empty((F, n, n, n), device=dev).permute(1, 2, 3, 0)  # frame-major storage
+    x.copy_(torch.from_numpy(x4))
+    c = torch.zeros_like(x)
+    y = torch.zeros((T, N, N), device=dev).permute(1, 2, 0)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, device=dev)
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    pj, bpj = [], []
+    for r in range(reps + 2):
+        flush.fill_(1.0)
+        y.zero_()
+        c.zero_()
+        e[0].record()
+        siddon.run_device("pjt", y, x, views, mh, T, obstacle="sun")
+        e[1].record()
+        flush.fill_(1.0)
+        e[2].record()
+        siddon.run_device("bpjt", y, c, views, mh, T, obstacle="sun")
+        e[3].record()
+        torch.cuda.synchronize()
+        if r >= 2:
+            pj.append(e[0].elapsed_time(e[1]))
+            bpj.append(e[2].elapsed_time(e[3]))
+    rays = N * N * T
+    P = lo_wrapper.siddon4d_lo(vh, ch, ng=T // F, obstacle="sun", dtype=np.float32, device=dev)
+    b = P.backproject(y.contiguous())
+    A = cg.NormalOperator(P, lam=1e-2, temporal=1e-2)
+    cg.cg(A, b, maxiter=2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = cg.cg(A, b, maxiter=cg_iters, graph=True)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    return {"workload": "128^3 x 28 frames (frame-major), 784 views of 256^2 over 0-360 deg, view -> frame v // 28, sun",
+            "rays_per_step": rays, "pjt_ms": statistics.mean(pj), "bpjt_ms": statistics.mean(bpj),
+            "rays_per_s": rays / ((statistics.mean(pj) + statistics.mean(bpj)) / 1000.0),
+            "cg": {"iterations": cg_iters, "it_per_s": cg_iters / dt, "seconds": dt,
+                   "terms": "P^T P + 1e-2 I + 1e-2 D_t^T D_t (4-D operator, frame-major cube)",
+                   "relative_residual": res.residuals[-1]}}
 
 
 def measure_batched(dev, n_jobs=32, iters=20, seed=0):

@@ -127,6 +127,13 @@ class SegmentOps:
                                              self._p(self.seg), self.n, self._st()))
 
 
+def dense(t):
+    """True when ``t`` covers its storage without gaps: contiguous after a
+    permutation of its axes (e.g. a frame-major 4-D cube)."""
+    order = sorted(range(t.dim()), key=lambda d: -t.stride(d))
+    return t.permute(*order).is_contiguous()
+
+
 def cg(A, b, x0=None, maxiter=10, tol=0.0, graph=False):
     """Solve A x = b (A symmetric positive definite, callable on device tensors).
 
@@ -137,11 +144,12 @@ def cg(A, b, x0=None, maxiter=10, tol=0.0, graph=False):
     vector updates as single float32 FMAs).
     """
     dev = b.device
-    if b.dtype != torch.float32 or not b.is_contiguous():
-        raise ValueError("cg takes a contiguous float32 right-hand side")
+    if b.dtype != torch.float32 or not dense(b):
+        raise ValueError("cg takes a dense float32 right-hand side (contiguous up to a permutation of axes)")
     ops = SegmentOps([0, b.numel()], dev)
-    x = torch.zeros_like(b) if x0 is None else x0.clone()
-    r = b - A(x) if x0 is not None else b.clone()
+    # every vector shares b's layout (the vector kernels run on flat storage)
+    x = torch.zeros_like(b) if x0 is None else torch.empty_like(b).copy_(x0)
+    r = torch.empty_like(b).copy_(b - A(x)) if x0 is not None else b.clone()
     p = r.clone()
     rr = torch.zeros(1, dtype=torch.float64, device=dev)
     rr_new = torch.zeros_like(rr)
@@ -154,7 +162,9 @@ def cg(A, b, x0=None, maxiter=10, tol=0.0, graph=False):
     k_dev = torch.zeros((), dtype=torch.int64, device=dev)
 
     def step():
-        Ap = A(p).contiguous()
+        Ap = A(p)
+        if Ap.stride() != p.stride():  # the vector kernels run on flat storage
+            Ap = torch.empty_like(p).copy_(Ap)
         ops.dot(p, Ap, pAp)
         ops.update_x(x, r, p, Ap, rr, pAp)
         ops.dot(r, r, rr_new)

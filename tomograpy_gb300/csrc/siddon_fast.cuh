@@ -57,6 +57,9 @@ namespace tg {
 #ifndef TG_BPJ_MIN_BLOCKS
 #define TG_BPJ_MIN_BLOCKS 4
 #endif
+#ifndef TG_BPJ_PAIR
+#define TG_BPJ_PAIR 0
+#endif
 #ifndef TG_PJ_DRIFT
 #define TG_PJ_DRIFT 1
 #endif
@@ -638,7 +641,24 @@ __device__ __forceinline__ void trace_fast(const Geometry &G, const tg_image_hea
       acc += part;
     } else {
 #pragma unroll
-      for (int s = 0; s < kBatch; ++s) accumulate<MODE, DET, IDX>(L[s], o[s], cin, cout, aout, yv, yq, qs, acc);
+      for (int s = 0; s < kBatch; ++s) {
+        if (!DET && TG_BPJ_PAIR) {
+          // neighbouring pixels (lanes l, l ^ 1) are often in the same voxel
+          // at the same step: the even lane adds both contributions
+          const unsigned active = __activemask();
+          const bool partner = (active >> (lane ^ 1)) & 1u;
+          const float v = L[s] * yv;
+          const IDX po = __shfl_xor_sync(active, o[s], 1);
+          const float pv = __shfl_xor_sync(active, v, 1);
+          if (partner && po == o[s]) {
+            if (!(lane & 1)) red_add_f32(cout + o[s], v + pv);
+          } else {
+            red_add_f32(cout + o[s], v);
+          }
+        } else {
+          accumulate<MODE, DET, IDX>(L[s], o[s], cin, cout, aout, yv, yq, qs, acc);
+        }
+      }
     }
   }
   // Remaining steps before tstop, one at a time.

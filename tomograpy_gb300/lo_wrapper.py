@@ -84,6 +84,16 @@ class Siddon(LinearOperator):
             t = torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=self.dtype))).to(self.device)
         return t.reshape(shape)
 
+    def new_cube(self):
+        """A zeroed cube of the operator's shape.  4-D cubes are stored
+        frame-major (each frame contiguous, presented as (n0, n1, n2, F)
+        through strides): a frame's views then gather from one contiguous,
+        L2-resident block instead of frames interleaved in every sector."""
+        if self.four_d:
+            n0, n1, n2, F = self.cube_shape
+            return torch.zeros((F, n0, n1, n2), dtype=self.tdtype, device=self.device).permute(1, 2, 3, 0)
+        return torch.zeros(self.cube_shape, dtype=self.tdtype, device=self.device)
+
     def project(self, x, out=None):
         """y = P x.  ``x``: cube (CUDA or host tensor / array).  Returns a CUDA
         tensor, or fills ``out`` (device or host tensor) and returns it."""
@@ -96,7 +106,7 @@ class Siddon(LinearOperator):
     def backproject(self, y, out=None):
         """x = P^T y.  ``y``: data stack (CUDA or host tensor / array)."""
         yd = self._dev(y, self.data_shape)
-        x = torch.zeros(self.cube_shape, dtype=self.tdtype, device=self.device)
+        x = self.new_cube()
         if self.deterministic and self.tdtype == torch.float32:
             from . import _lib
             need = _lib.load().tg_deterministic_workspace_bytes(

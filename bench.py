@@ -63,6 +63,23 @@ def parse():
     return ap.parse_args()
 
 
+def slowest_rank_ms(ms, world, device):
+    """Step time of the job: the maximum over ranks (all ranks get it)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank, ms, world):
+    """Whole-job rate of `world` independent replicas that each process
+    `units_per_rank` units per step in `ms` (the slowest rank's time)."""
+    return world * units_per_rank / (ms / 1000.0)
+
+
 def dist_env():
     return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
             int(os.environ.get("LOCAL_RANK", 0)))
@@ -288,12 +305,8 @@ def run_ours(args):
     if world > 1:
         dist.barrier()
     clk = clocks.stop()
-    ms = statistics.mean(step_ms)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * rays / (ms / 1000.0)
+    ms = slowest_rank_ms(statistics.mean(step_ms), world, dev)
+    value = replica_throughput(rays, ms, world)
 
     # roofline of the dominant kernel (algorithmic bytes per launch / its mean duration)
     peak, peak_kind = measured_peak()
@@ -338,8 +351,10 @@ def run_ours(args):
         four_d = measure_4d(dev)
     if rank == 0 and not args.no_batched:
         batched = measure_batched(dev)
+        batched["small_jobs"] = measure_batched(dev, n_jobs=256, mix=SMALL_MIX)
     if rank == 0 and not args.no_served:
         served = measure_served(dev, args.served_jobs)
+        served["small_jobs"] = measure_served(dev, 500, rate=1000.0, mix=SMALL_MIX, large=0.0)
 
     if rank == 0:
         out = {
@@ -410,7 +425,7 @@ def measure_4d(dev, reps=5, cg_iters=30):
     cg.cg(A, b, maxiter=2)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    res = cg.cg(A, b, maxiter=cg_iters, graph=True)
+    res = cg.cg(A, b, maxiter=cg_iters)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     return {"workload": "128^3 x 28 frames (frame-major), 784 views of 256^2 over 0-360 deg, view -> frame v // 28, sun",
@@ -421,16 +436,20 @@ def measure_4d(dev, reps=5, cg_iters=30):
                    "relative_residual": res.residuals[-1]}}
 
 
-def measure_batched(dev, n_jobs=32, iters=20, seed=0):
+SMALL_MIX = dict(edges=(16, 24, 32, 48), sides=(32, 48, 64), views=(8, 32))
+
+
+def measure_batched(dev, n_jobs=32, iters=20, seed=0, mix=None):
     """Uneven multi-job batch: 32 seeded reconstructions (cube edge in
-    {32..192}, 16-256 views of 64-512 px, d in [150, 230]), 20 CG iterations
-    on (P^T P + 1e-2 I) x = P^T y each, solved (a) together with one packed
-    launch per direction per iteration, CUDA-graph captured, tile shape
-    autotuned, and (b) one after another with the single-job operator."""
+    {32..192}, 16-256 views of 64-512 px, d in [150, 230]; or the sizes of
+    `mix`), 20 CG iterations on (P^T P + 1e-2 I) x = P^T y each, solved (a)
+    together with one packed launch per direction per iteration, CUDA-graph
+    captured, tile shape autotuned, and (b) one after another with the
+    single-job operator."""
     import torch
 
     from tomograpy_gb300 import batch, synthetic
-    specs = synthetic.uneven_specs(n_jobs, seed=seed)
+    specs = synthetic.uneven_specs(n_jobs, seed=seed, **(mix or {}))
     jobs = [synthetic.make_job(s, seed=k) for k, s in enumerate(specs)]
     pack = batch.PackedJobs(jobs, obstacle="sun", device=dev)
     x = pack.new_cube()
@@ -453,26 +472,34 @@ def measure_batched(dev, n_jobs=32, iters=20, seed=0):
     diff = max(float((pack.cube_view(xb, k) - xs[k]).abs().max() / xs[k].abs().max().clamp_min(1e-30))
                for k in range(n_jobs))
     rays = sum(int(j.data_shape[0] * j.data_shape[1] * j.data_shape[2]) for j in jobs)
-    return {"workload": "uneven batch: %d seeded jobs (edges 32-192, 16-256 views, 64-512 px), %d CG iterations, "
-                        "sun" % (n_jobs, iters),
+    sizes = ("edges %s, %d-%d views, %s px" % (mix["edges"], mix["views"][0], mix["views"][1], mix["sides"])
+             if mix else "edges 32-192, 16-256 views, 64-512 px")
+    return {"workload": "uneven batch: %d seeded jobs (%s), %d CG iterations, sun" % (n_jobs, sizes, iters),
             "rays_per_iteration": rays, "rows_per_warp": pack.rows_per_warp,
             "batched_cg_it_per_s": n_jobs * iters / tb, "plain_cg_it_per_s": n_jobs * iters / ts,
             "speedup": ts / tb, "batched_s": tb, "plain_s": ts, "max_rel_diff_vs_plain": diff,
             "plain": "one job after another: single-job operator + the same CG kernels (no graph)"}
 
 
-def measure_served(dev, n_jobs=60, rate=20.0, seed=0):
+def measure_served(dev, n_jobs=60, rate=20.0, seed=0, mix=None, large=0.1):
     """Serving stream sample: Poisson arrivals (20 jobs/s, seeded), sizes as the
-    uneven batch plus 10 % large jobs (256^3, 360 x 512^2), 20 CG iterations
-    or relative residual 1e-4 each; continuous batching vs a FIFO plain loop."""
+    uneven batch (or `mix`) plus a fraction `large` of 256^3 x 360 x 512^2
+    jobs, 20 CG iterations or relative residual 1e-4 each; continuous
+    batching vs a FIFO plain loop."""
     import numpy as np
 
     from tomograpy_gb300 import serve, synthetic
     rng = np.random.default_rng(seed + 99)
-    specs = synthetic.uneven_specs(n_jobs, seed=seed + 1)
+    specs = synthetic.uneven_specs(n_jobs, seed=seed + 1, **(mix or {}))
     for k in range(n_jobs):
-        if rng.random() < 0.1:
+        if rng.random() < large:
             specs[k] = dict(synthetic.CONFIGS["recon256"])
+    # warm-up (untimed): the first launches of every kernel variant and the
+    # first pinned allocations of a process would otherwise land in the stream
+    warm = serve.poisson_requests(specs[:8], rate=1e6, seed=seed, max_iters=3, tol=1e-4, device=dev)
+    serve.Server(device=dev).run(warm)
+    serve.fifo_plain(serve.poisson_requests(specs[:8], rate=1e6, seed=seed, max_iters=3, tol=1e-4, device=dev),
+                     device=dev)
     reqs = serve.poisson_requests(specs, rate=rate, seed=seed, max_iters=20, tol=1e-4, device=dev)
     srv = serve.Server(device=dev)
     s = srv.run(reqs)
@@ -480,10 +507,13 @@ def measure_served(dev, n_jobs=60, rate=20.0, seed=0):
     f = serve.fifo_plain(reqs2, device=dev)
     diff = max(float((a.result - c.result).abs().max() / c.result.abs().max().clamp_min(1e-30))
                for a, c in zip(reqs, reqs2))
-    return {"workload": "serving stream: %d Poisson requests at %.0f jobs/s, uneven sizes + 10%% 256^3 x 360 x "
-                        "512^2, 20 CG iterations or residual 1e-4" % (n_jobs, rate),
+    sizes = ("small uneven sizes (edges %s, %d-%d views, %s px)" % (mix["edges"], mix["views"][0], mix["views"][1],
+                                                                      mix["sides"]) if mix else "uneven sizes")
+    return {"workload": "serving stream: %d Poisson requests at %.0f jobs/s, %s + %d%% 256^3 x 360 x 512^2, "
+                        "20 CG iterations or residual 1e-4" % (n_jobs, rate, sizes, round(100 * large)),
             "served": s, "fifo_plain": f, "cg_it_per_s_ratio": s["cg_it_per_s"] / f["cg_it_per_s"],
-            "max_inflight": srv.max_inflight, "max_rel_diff_vs_plain": diff}
+            "max_inflight": srv.max_inflight, "max_rel_diff_vs_plain": diff,
+            "server_host_s": srv.host_s, "server_rebuilds": srv.rebuilds}
 
 
 def run_profile_case():

@@ -223,6 +223,11 @@ typedef struct {
 size_t tg_packed_plan_bytes(int32_t n_jobs);
 tg_status tg_packed_plan(const tg_job *jobs, int32_t n_jobs, int32_t rows_per_warp, int32_t four_d, void *plan,
                          size_t plan_bytes, tg_packed_info *info);
+/* Same plan written to host memory (no device work, no synchronisation): the
+ * caller uploads it, e.g. with cudaMemcpyAsync from pinned memory on its
+ * stream, so re-planning does not stall a stream that is busy. */
+tg_status tg_packed_plan_host(const tg_job *jobs, int32_t n_jobs, int32_t rows_per_warp, int32_t four_d,
+                              void *host_plan, size_t plan_bytes, tg_packed_info *info);
 tg_status tg_packed_projector(const void *plan, const tg_packed_info *info, int32_t mode, int32_t obstacle,
                               void *stream);
 

@@ -54,6 +54,8 @@ def _bind(L):
     L.tg_packed_plan_bytes.restype = SZ
     L.tg_packed_plan.argtypes = [P, I32, I32, I32, P, SZ, P]
     L.tg_packed_plan.restype = ctypes.c_int
+    L.tg_packed_plan_host.argtypes = [P, I32, I32, I32, P, SZ, P]
+    L.tg_packed_plan_host.restype = ctypes.c_int
     L.tg_packed_projector.argtypes = [P, P, I32, I32, P]
     L.tg_packed_projector.restype = ctypes.c_int
     L.tg_segmented_workspace_bytes.argtypes = [I32]

@@ -295,13 +295,35 @@ size_t tg_packed_plan_bytes(int32_t n_jobs) {
   return tg::packed_records_offset(n_jobs) + (((size_t)n_jobs * tg::packed_job_bytes() + 255) & ~(size_t)255);
 }
 
+static tg_status build_packed_plan(const tg_job *jobs, int32_t n_jobs, int32_t rows_per_warp, int32_t four_d,
+                                   unsigned char *host, tg_packed_info *info);
+
 tg_status tg_packed_plan(const tg_job *jobs, int32_t n_jobs, int32_t rows_per_warp, int32_t four_d, void *plan,
                          size_t plan_bytes, tg_packed_info *info) {
   if (!info) return fail(TG_EINVAL, "info is NULL");
   if (n_jobs <= 0 || !jobs) return fail(TG_EINVAL, "no jobs");
+  if (!plan || plan_bytes < tg_packed_plan_bytes(n_jobs)) return fail(TG_ENOMEM, "plan buffer too small");
+  std::vector<unsigned char> host(tg_packed_plan_bytes(n_jobs), 0);
+  tg_status st = build_packed_plan(jobs, n_jobs, rows_per_warp, four_d, host.data(), info);
+  if (st != TG_OK) return st;
+  cudaError_t e = cudaMemcpy(plan, host.data(), host.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return launch_status(e, "plan upload");
+  return TG_OK;
+}
+
+tg_status tg_packed_plan_host(const tg_job *jobs, int32_t n_jobs, int32_t rows_per_warp, int32_t four_d,
+                              void *host_plan, size_t plan_bytes, tg_packed_info *info) {
+  if (!info) return fail(TG_EINVAL, "info is NULL");
+  if (n_jobs <= 0 || !jobs) return fail(TG_EINVAL, "no jobs");
+  if (!host_plan || plan_bytes < tg_packed_plan_bytes(n_jobs)) return fail(TG_ENOMEM, "plan buffer too small");
+  std::memset(host_plan, 0, tg_packed_plan_bytes(n_jobs));
+  return build_packed_plan(jobs, n_jobs, rows_per_warp, four_d, (unsigned char *)host_plan, info);
+}
+
+static tg_status build_packed_plan(const tg_job *jobs, int32_t n_jobs, int32_t rows_per_warp, int32_t four_d,
+                                   unsigned char *host, tg_packed_info *info) {
   if (rows_per_warp != 1 && rows_per_warp != 2 && rows_per_warp != 4)
     return fail(TG_EINVAL, "rows_per_warp must be 1, 2 or 4");
-  if (!plan || plan_bytes < tg_packed_plan_bytes(n_jobs)) return fail(TG_ENOMEM, "plan buffer too small");
   const int rows = rows_per_warp * tg::kRows;
   struct Item {
     double work;
@@ -323,20 +345,17 @@ tg_status tg_packed_plan(const tg_job *jobs, int32_t n_jobs, int32_t rows_per_wa
     order[j] = {(double)J.n_views * J.n1 * J.n2 * (double)(J.map_shape[0] + J.map_shape[1] + J.map_shape[2]), j};
   }
   std::stable_sort(order.begin(), order.end(), [](const Item &a, const Item &b) { return a.work > b.work; });
-  std::vector<unsigned char> host(tg_packed_plan_bytes(n_jobs), 0);
   const size_t rec0 = tg::packed_records_offset(n_jobs);
   long long tiles = 0;
   for (int k = 0; k < n_jobs; ++k) {
     const int j = order[k].idx;
     const tg_job &J = jobs[j];
     const int gx = (int)((J.n2 + 31) / 32), gy = (int)((J.n1 + rows - 1) / rows);
-    std::memcpy(host.data() + (size_t)k * sizeof(long long), &tiles, sizeof(long long));
-    tg::packed_fill(host.data() + rec0 + (size_t)k * tg::packed_job_bytes(), geoms[j], J.data, J.map, tiles, gx, gy);
+    std::memcpy(host + (size_t)k * sizeof(long long), &tiles, sizeof(long long));
+    tg::packed_fill(host + rec0 + (size_t)k * tg::packed_job_bytes(), geoms[j], J.data, J.map, tiles, gx, gy);
     tiles += (long long)gx * gy * J.n_views;
   }
   if (tiles > 2147483647LL) return fail(TG_EUNSUPPORTED, "packed launch of %lld CTAs is too large", tiles);
-  cudaError_t e = cudaMemcpy(plan, host.data(), host.size(), cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) return launch_status(e, "plan upload");
   info->n_jobs = n_jobs;
   info->rows_per_warp = rows_per_warp;
   info->four_d = four_d != 0;

@@ -15,7 +15,6 @@ jobs/s and CG-iterations/s.  :func:`fifo_plain` is the baseline: the same
 requests served one at a time in arrival order with the plain single-job path.
 """
 import ctypes
-import heapq
 import time
 
 import numpy as np
@@ -77,14 +76,71 @@ class Request:
         self.residual = None
 
 
+class PinnedStaging:
+    """Host -> device uploads that never stall the stream: arrays are copied
+    into one preallocated pinned buffer (bump allocation) and sent with an
+    asynchronous copy; when the buffer wraps, the host waits for the copies
+    staged since the previous wrap (rare with a buffer of a few MB)."""
+
+    def __init__(self, nbytes=8 << 20):
+        self.buf = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+        self.host = self.buf.numpy()
+        self.head = 0
+        self.events = []
+
+    def upload(self, array, dev):
+        a = np.ascontiguousarray(array)
+        nb = a.nbytes
+        if nb > self.buf.numel():
+            return torch.from_numpy(a).to(dev)
+        if self.head + nb > self.buf.numel():
+            for ev in self.events:
+                ev.synchronize()
+            self.events.clear()
+            self.head = 0
+        self.host[self.head:self.head + nb] = a.reshape(-1).view(np.uint8)
+        out = torch.empty(nb, dtype=torch.uint8, device=dev)
+        out.copy_(self.buf[self.head:self.head + nb], non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record()
+        self.events.append(ev)
+        self.head += (nb + 255) & ~255
+        return out.view(_TORCH_DTYPES[a.dtype.str]).view(a.shape)
+
+
+_TORCH_DTYPES = {}
+
+
+def _torch_dtypes():
+    if not _TORCH_DTYPES and torch is not None:
+        _TORCH_DTYPES.update({np.dtype(np.int64).str: torch.int64, np.dtype(np.uint8).str: torch.uint8,
+                              np.dtype(np.float32).str: torch.float32, np.dtype(np.float64).str: torch.float64})
+
+
+class _Slot:
+    """Device residency of one admitted request."""
+
+    def __init__(self, req, c, d, views, slot, nc, nd):
+        self.req, self.c, self.d, self.views, self.slot, self.nc, self.nd = req, c, d, views, slot, nc, nd
+        self.rec = {}       # packed job records (bytes) per direction
+        self.converged = False
+
+
 class Server:
     """Continuous-batching CG server on one GPU.
 
     ``budget_bytes`` bounds the device memory of resident jobs (cube vectors
-    x, r, p, Ap and the data stack of every in-flight job)."""
+    x, r, p, Ap and the data stack of every in-flight job; default: half of
+    the free device memory).  The host never waits for the GPU inside the
+    loop except to keep at most two steps queued: plans and segment tables
+    go up from pinned memory, residual norms and results come back through
+    pinned memory and CUDA events.  A job retires after ``max_iters``
+    iterations, or once the host sees its relative residual at or below
+    ``tol`` (read one or two steps late, so such a job may run one or two
+    iterations past its tolerance)."""
 
     def __init__(self, budget_bytes=None, lam=1e-2, obstacle="sun", rows_per_warp=4, device=None,
-                 cube_fraction=0.4, max_rays=1 << 23, max_wait=1.0):
+                 cube_fraction=0.4, max_rays=1 << 23, max_wait=1.0, max_slots=4096):
         self.L = B._bind(_lib.load())
         self.dev = device or S._device()
         self.lam = float(lam)
@@ -104,16 +160,28 @@ class Server:
         self.data = torch.zeros(self.data_elems, dtype=torch.float32, device=self.dev)
         self.cube_arena = Arena(self.cube_elems)
         self.data_arena = Arena(self.data_elems)
-        self.inflight = []       # list of (request, cube range, data range, views_dev)
+        self.bb_all = torch.ones(max_slots, dtype=torch.float64, device=self.dev)   # ||b||^2 per slot
+        self.free_slots = list(range(max_slots))[::-1]
+        self.inflight = []       # _Slot list, in plan order
         self.dirty = True
         self.iterations = 0
         self.completed = []
         self.max_inflight = 0
+        _torch_dtypes()
+        self.staging = PinnedStaging()
+        self._rel_ring = torch.empty((8, max_slots), dtype=torch.float64, pin_memory=True)
+        self._nsteps = 0
+        self._steps = []         # queued steps: (event, pinned residuals, slots)
+        self._results = []       # (request, pinned cube, event)
+        self.host_s = {"admit": 0.0, "rebuild": 0.0, "step": 0.0, "retire": 0.0, "collect": 0.0}
+        self.rebuilds = 0
 
     # admission -------------------------------------------------------------
     def try_admit(self, req):
         nc = int(np.prod(req.job.cube_shape))
         nd = int(np.prod(req.job.data_shape))
+        if not self.free_slots:
+            return False
         c = self.cube_arena.alloc(nc)
         if c is None:
             return False
@@ -121,7 +189,8 @@ class Server:
         if d is None:
             self.cube_arena.release(*c)
             return False
-        views = S.upload_views(req.job.view_headers, None, self.dev)
+        views = self.staging.upload(S.pack_views(req.job.view_headers).view(np.uint8).reshape(-1), self.dev)
+        job = _Slot(req, c, d, views, self.free_slots.pop(), nc, nd)
         n1, n2, T = req.job.data_shape
         dv = self.data[d[0]:d[0] + nd].view(T, n1, n2).permute(1, 2, 0)
         host = req.data if torch.is_tensor(req.data) else torch.from_numpy(np.ascontiguousarray(req.data))
@@ -130,13 +199,32 @@ class Server:
         # data slot is the job's scratch for P p
         r = self.vec["r"][c[0]:c[0] + nc]
         r.zero_()
-        S.run_device("bpj", dv, r.view(*req.job.cube_shape), views, S.pack_map_header(req.job.cube_header), T,
-                     obstacle=self.obstacle)
+        mh = S.pack_map_header(req.job.cube_header)
+        S.run_device("bpj", dv, r.view(*req.job.cube_shape), views, mh, T, obstacle=self.obstacle)
         self.vec["p"][c[0]:c[0] + nc].copy_(r)
         self.vec["x"][c[0]:c[0] + nc].zero_()
-        req.bb = float(torch.dot(r.double(), r.double()))
+        rd = r.double()
+        self.bb_all[job.slot:job.slot + 1].copy_(torch.dot(rd, rd).clamp_min(1e-300).view(1))
+        for key, vecname in (("pj", "p"), ("bpj", "a")):
+            cv = self.vec[vecname][c[0]:c[0] + nc].view(*req.job.cube_shape)
+            J = B.TgJob()
+            J.map_header = mh
+            J.views = views.data_ptr()
+            J.n_views = T
+            J.n1, J.n2 = n1, n2
+            for k in range(3):
+                J.data_strides[k] = dv.stride()[k]
+                J.map_shape[k] = cv.shape[k]
+                J.map_strides[k] = cv.stride()[k]
+            J.map_shape[3] = 1
+            J.map_strides[3] = 0
+            J.mask = None
+            J.mask_dtype = _lib.TG_U8
+            J.data = dv.data_ptr()
+            J.map = cv.data_ptr()
+            job.rec[key] = bytes(J)
         req.t_admit = time.perf_counter() - self.t_start
-        self.inflight.append((req, c, d, views))
+        self.inflight.append(job)
         self.max_inflight = max(self.max_inflight, len(self.inflight))
         self.dirty = True
         return True
@@ -147,61 +235,46 @@ class Server:
         n = len(self.inflight)
         seg = np.zeros(2 * n, dtype=np.int64)
         dseg = np.zeros(2 * n, dtype=np.int64)
-        for k, (req, c, d, views) in enumerate(self.inflight):
-            seg[2 * k], seg[2 * k + 1] = c[0], c[0] + int(np.prod(req.job.cube_shape))
-            dseg[2 * k], dseg[2 * k + 1] = d[0], d[0] + int(np.prod(req.job.data_shape))
-        self.cube_ops = SegmentOps(torch.from_numpy(seg).to(self.dev), self.dev)
-        self.data_ops = SegmentOps(torch.from_numpy(dseg).to(self.dev), self.dev)
+        for k, job in enumerate(self.inflight):
+            seg[2 * k], seg[2 * k + 1] = job.c[0], job.c[0] + job.nc
+            dseg[2 * k], dseg[2 * k + 1] = job.d[0], job.d[0] + job.nd
+        self.cube_ops = SegmentOps(self.staging.upload(seg, self.dev), self.dev)
+        self.data_ops = SegmentOps(self.staging.upload(dseg, self.dev), self.dev)
         self.n = n
         self.plans = {}
-        for key, vecname in (("pj", "p"), ("bpj", "a")):
-            arr = (B.TgJob * n)()
-            for k, (req, c, d, views) in enumerate(self.inflight):
-                n1, n2, T = req.job.data_shape
-                nd = n1 * n2 * T
-                dv = self.data[d[0]:d[0] + nd].view(T, n1, n2).permute(1, 2, 0)
-                cv = self.vec[vecname][c[0]:c[0] + int(np.prod(req.job.cube_shape))].view(*req.job.cube_shape)
-                J = arr[k]
-                J.map_header = S.pack_map_header(req.job.cube_header)
-                J.views = views.data_ptr()
-                J.n_views = T
-                J.n1, J.n2 = n1, n2
-                for a in range(3):
-                    J.data_strides[a] = dv.stride()[a]
-                    J.map_shape[a] = cv.shape[a]
-                    J.map_strides[a] = cv.stride()[a]
-                J.map_shape[3] = 1
-                J.map_strides[3] = 0
-                J.mask = None
-                J.mask_dtype = _lib.TG_U8
-                J.data = dv.data_ptr()
-                J.map = cv.data_ptr()
+        for key in ("pj", "bpj"):
+            arr = (B.TgJob * n).from_buffer_copy(b"".join(job.rec[key] for job in self.inflight))
             nbytes = self.L.tg_packed_plan_bytes(n)
-            buf = torch.empty(nbytes, dtype=torch.uint8, device=self.dev)
+            host = np.empty(nbytes, dtype=np.uint8)
             info = B.TgPackedInfo()
-            _lib.check(self.L.tg_packed_plan(arr, n, self.rpw, 0, B._ptr(buf), nbytes, ctypes.byref(info)))
-            self.plans[key] = (buf, info, arr)
+            _lib.check(self.L.tg_packed_plan_host(arr, n, self.rpw, 0, ctypes.c_void_p(host.ctypes.data), nbytes,
+                                                  ctypes.byref(info)))
+            self.plans[key] = (self.staging.upload(host, self.dev), info)
         # per-job scalars: rr = r.r recomputed from the resident vectors (the
-        # segmented dot of a segment does not depend on the other segments)
+        # segmented dot of a range does not depend on the other ranges)
         self.rr = torch.zeros(n, dtype=torch.float64, device=self.dev)
         self.rr_new = torch.zeros_like(self.rr)
         self.pAp = torch.zeros_like(self.rr)
         self.cube_ops.dot(self.vec["r"], self.vec["r"], self.rr)
-        self.bb = torch.tensor([max(req.bb, 1e-300) for req, *_ in self.inflight], dtype=torch.float64,
-                               device=self.dev)
+        slots = self.staging.upload(np.array([job.slot for job in self.inflight], dtype=np.int64), self.dev)
+        self.bb = self.bb_all.index_select(0, slots)
         self.dirty = False
 
     # one CG iteration for every in-flight job ----------------------------------
     def step(self):
         if self.dirty:
+            t0 = time.perf_counter()
             self._rebuild()
+            self.rebuilds += 1
+            self.host_s["rebuild"] += time.perf_counter() - t0
+        t0 = time.perf_counter()
         L, st, ops, v = self.L, B._stream(), self.cube_ops, self.vec
         ob = _lib.OBSTACLES[self.obstacle]
         self.data_ops.axpby(self.data, None, 0.0, 0.0)            # scratch = 0
-        buf, info, _ = self.plans["pj"]
+        buf, info = self.plans["pj"]
         _lib.check(L.tg_packed_projector(B._ptr(buf), ctypes.byref(info), _lib.TG_PJ, ob, st))   # P p
         ops.axpby(v["a"], None, 0.0, 0.0)
-        buf, info, _ = self.plans["bpj"]
+        buf, info = self.plans["bpj"]
         _lib.check(L.tg_packed_projector(B._ptr(buf), ctypes.byref(info), _lib.TG_BPJ, ob, st))  # P^T P p
         if self.lam:
             ops.axpby(v["a"], v["p"], self.lam, 1.0)
@@ -209,35 +282,63 @@ class Server:
         ops.update_x(v["x"], v["r"], v["p"], v["a"], self.rr, self.pAp)
         ops.dot(v["r"], v["r"], self.rr_new)
         ops.update_p(v["p"], v["r"], self.rr, self.rr_new)
+        rel = self._rel_ring[self._nsteps % self._rel_ring.shape[0], :self.n]   # <= 3 steps outstanding
+        self._nsteps += 1
+        rel.copy_(torch.sqrt(self.rr / self.bb), non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record()
+        self._steps.append((ev, rel, list(self.inflight)))
         self.iterations += self.n
-        for req, *_ in self.inflight:
-            req.iters += 1
+        for job in self.inflight:
+            job.req.iters += 1
+        self.host_s["step"] += time.perf_counter() - t0
+
+    def _read_residuals(self, keep_queued=2):
+        """Consume the residuals of finished steps, waiting only while more
+        than `keep_queued` steps are queued."""
+        while self._steps and (len(self._steps) > keep_queued or self._steps[0][0].query()):
+            ev, rel, jobs = self._steps.pop(0)
+            ev.synchronize()
+            vals = rel.numpy().copy()
+            for job, r in zip(jobs, vals):
+                job.req.residual = float(r)
+                if r <= job.req.tol:
+                    job.converged = True
 
     def retire(self):
-        """Move converged / exhausted jobs out; returns how many left."""
-        rel = torch.sqrt(self.rr / self.bb).cpu().numpy()
+        """Move converged / exhausted jobs out (results copied back
+        asynchronously); returns how many left."""
+        self._read_residuals()
         keep, done = [], []
-        for k, item in enumerate(self.inflight):
-            req = item[0]
-            if rel[k] <= req.tol or req.iters >= req.max_iters:
-                done.append((item, float(rel[k])))
-            else:
-                keep.append(item)
-        for (req, c, d, views), res in done:
-            nc = int(np.prod(req.job.cube_shape))
-            req.result = self.vec["x"][c[0]:c[0] + nc].view(*req.job.cube_shape).cpu()
-            req.residual = res
-            req.t_done = time.perf_counter() - self.t_start
-            self.cube_arena.release(*c)
-            self.data_arena.release(*d)
-            self.completed.append(req)
+        for job in self.inflight:
+            (done if job.converged or job.req.iters >= job.req.max_iters else keep).append(job)
+        for job in done:
+            req = job.req
+            out = torch.empty(job.nc, dtype=torch.float32, pin_memory=True)
+            out.copy_(self.vec["x"][job.c[0]:job.c[0] + job.nc], non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record()
+            self._results.append((req, out.view(*req.job.cube_shape), ev))
+            self.cube_arena.release(*job.c)   # stream order protects the copy
+            self.data_arena.release(*job.d)
+            self.free_slots.append(job.slot)
         if done:
             self.inflight = keep
             self.dirty = True
         return len(done)
 
+    def _collect(self, wait=False):
+        while self._results and (wait or self._results[0][2].query()):
+            req, out, ev = self._results.pop(0)
+            ev.synchronize()
+            req.result = out
+            req.t_done = time.perf_counter() - self.t_start
+            if req.residual is None:
+                req.residual = float("nan")
+            self.completed.append(req)
+
     def _rays_inflight(self):
-        return sum(int(np.prod(r.job.data_shape)) for r, *_ in self.inflight)
+        return sum(job.nd for job in self.inflight)
 
     def _admit(self, queue, now):
         """Admit queued requests: in arrival order while the in-flight rays stay
@@ -268,7 +369,13 @@ class Server:
             now = time.perf_counter() - self.t_start
             while pending and pending[0].arrival <= now:
                 queue.append(pending.pop(0))
+            t0 = time.perf_counter()
             self._admit(queue, now)
+            t1 = time.perf_counter()
+            self._collect()
+            t2 = time.perf_counter()
+            self.host_s["admit"] += t1 - t0
+            self.host_s["collect"] += t2 - t1
             if not self.inflight:
                 if queue:
                     raise RuntimeError("request %d does not fit the memory budget" % queue[0].id)
@@ -276,7 +383,11 @@ class Server:
                     time.sleep(max(0.0, pending[0].arrival - (time.perf_counter() - self.t_start)))
                 continue
             self.step()
+            t0 = time.perf_counter()
             self.retire()
+            self.host_s["retire"] += time.perf_counter() - t0
+        self._read_residuals(keep_queued=0)
+        self._collect(wait=True)
         torch.cuda.synchronize()
         return summarize(self.completed, time.perf_counter() - self.t_start, self.iterations)
 

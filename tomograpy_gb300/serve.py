@@ -160,7 +160,9 @@ class Server:
         self.data = torch.zeros(self.data_elems, dtype=torch.float32, device=self.dev)
         self.cube_arena = Arena(self.cube_elems)
         self.data_arena = Arena(self.data_elems)
-        self.bb_all = torch.ones(max_slots, dtype=torch.float64, device=self.dev)   # ||b||^2 per slot
+        # ||b||^2 per slot, written by the device at admission (read by the
+        # host only after a later step's event, so always complete)
+        self.bb_host = torch.ones(max_slots, dtype=torch.float64, pin_memory=True)
         self.free_slots = list(range(max_slots))[::-1]
         self.inflight = []       # _Slot list, in plan order
         self.dirty = True
@@ -171,7 +173,8 @@ class Server:
         self.staging = PinnedStaging()
         self._rel_ring = torch.empty((8, max_slots), dtype=torch.float64, pin_memory=True)
         self._nsteps = 0
-        self._steps = []         # queued steps: (event, pinned residuals, slots)
+        self._limbo = []         # (steps launched at retirement, slot)
+        self._steps = []         # queued steps: (event, pinned r.r, slots, step number)
         self._results = []       # (request, pinned cube, event)
         self.host_s = {"admit": 0.0, "rebuild": 0.0, "step": 0.0, "retire": 0.0, "collect": 0.0}
         self.rebuilds = 0
@@ -204,7 +207,7 @@ class Server:
         self.vec["p"][c[0]:c[0] + nc].copy_(r)
         self.vec["x"][c[0]:c[0] + nc].zero_()
         rd = r.double()
-        self.bb_all[job.slot:job.slot + 1].copy_(torch.dot(rd, rd).clamp_min(1e-300).view(1))
+        self.bb_host[job.slot:job.slot + 1].copy_(torch.dot(rd, rd).clamp_min(1e-300).view(1), non_blocking=True)
         for key, vecname in (("pj", "p"), ("bpj", "a")):
             cv = self.vec[vecname][c[0]:c[0] + nc].view(*req.job.cube_shape)
             J = B.TgJob()
@@ -256,8 +259,6 @@ class Server:
         self.rr_new = torch.zeros_like(self.rr)
         self.pAp = torch.zeros_like(self.rr)
         self.cube_ops.dot(self.vec["r"], self.vec["r"], self.rr)
-        slots = self.staging.upload(np.array([job.slot for job in self.inflight], dtype=np.int64), self.dev)
-        self.bb = self.bb_all.index_select(0, slots)
         self.dirty = False
 
     # one CG iteration for every in-flight job ----------------------------------
@@ -284,10 +285,10 @@ class Server:
         ops.update_p(v["p"], v["r"], self.rr, self.rr_new)
         rel = self._rel_ring[self._nsteps % self._rel_ring.shape[0], :self.n]   # <= 3 steps outstanding
         self._nsteps += 1
-        rel.copy_(torch.sqrt(self.rr / self.bb), non_blocking=True)
+        rel.copy_(self.rr, non_blocking=True)                      # r.r after the update
         ev = torch.cuda.Event()
         ev.record()
-        self._steps.append((ev, rel, list(self.inflight)))
+        self._steps.append((ev, rel, list(self.inflight), self._nsteps))
         self.iterations += self.n
         for job in self.inflight:
             job.req.iters += 1
@@ -297,13 +298,17 @@ class Server:
         """Consume the residuals of finished steps, waiting only while more
         than `keep_queued` steps are queued."""
         while self._steps and (len(self._steps) > keep_queued or self._steps[0][0].query()):
-            ev, rel, jobs = self._steps.pop(0)
+            ev, rel, jobs, step_no = self._steps.pop(0)
             ev.synchronize()
-            vals = rel.numpy().copy()
+            bb = self.bb_host.numpy()[[job.slot for job in jobs]]
+            vals = np.sqrt(rel.numpy() / bb)
             for job, r in zip(jobs, vals):
                 job.req.residual = float(r)
                 if r <= job.req.tol:
                     job.converged = True
+            # slots of retired jobs whose last step has now been read
+            while self._limbo and self._limbo[0][0] <= step_no:
+                self.free_slots.append(self._limbo.pop(0)[1])
 
     def retire(self):
         """Move converged / exhausted jobs out (results copied back
@@ -321,7 +326,9 @@ class Server:
             self._results.append((req, out.view(*req.job.cube_shape), ev))
             self.cube_arena.release(*job.c)   # stream order protects the copy
             self.data_arena.release(*job.d)
-            self.free_slots.append(job.slot)
+            # the slot (its ||b||^2 entry) is reused only after the residuals
+            # of every step this job took part in have been read
+            self._limbo.append((self._nsteps, job.slot))
         if done:
             self.inflight = keep
             self.dirty = True

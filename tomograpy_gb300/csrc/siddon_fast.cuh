@@ -42,9 +42,11 @@
 
 namespace tg {
 
-// Compile-time tuning per direction (measured on GB300 at 256^3 x 360 x 512^2:
-// the gather-bound projection prefers longer batches, the atomic-bound
-// backprojection more resident warps).
+// Compile-time tuning per direction (measured on GB300 at 256^3 x 360 x 512^2).
+// Both walk in drift batches (running-sum crossings, exact resynchronisation
+// per batch); the projection keeps a batch's gathers in registers (80
+// registers, 3 CTAs per SM), the backprojection issues each atomic at once
+// and so runs longer batches at 4 CTAs per SM (64 registers).
 #ifndef TG_PJ_BATCH
 #define TG_PJ_BATCH 20
 #endif
@@ -52,20 +54,22 @@ namespace tg {
 #define TG_PJ_MIN_BLOCKS 3
 #endif
 #ifndef TG_BPJ_BATCH
-#define TG_BPJ_BATCH 4
+#define TG_BPJ_BATCH 24
 #endif
 #ifndef TG_BPJ_MIN_BLOCKS
 #define TG_BPJ_MIN_BLOCKS 4
 #endif
-#ifndef TG_BPJ_PAIR
-#define TG_BPJ_PAIR 0
-#endif
 #ifndef TG_PJ_DRIFT
 #define TG_PJ_DRIFT 1
 #endif
+#ifndef TG_BPJ_DRIFT
+#define TG_BPJ_DRIFT 1
+#endif
 __host__ __device__ constexpr bool is_backprojection(int mode) { return mode == TG_BPJ || mode == TG_BPJT; }
 // running-sum crossings inside projection batches (drift_step)
-__host__ __device__ constexpr bool drift_batches(int mode) { return !is_backprojection(mode) && TG_PJ_DRIFT; }
+__host__ __device__ constexpr bool drift_batches(int mode) {
+  return is_backprojection(mode) ? TG_BPJ_DRIFT : TG_PJ_DRIFT;
+}
 // steps per batch of independent gathers / atomics
 __host__ __device__ constexpr int batch_steps(int mode) { return is_backprojection(mode) ? TG_BPJ_BATCH : TG_PJ_BATCH; }
 // CTAs per SM the register budget must allow
@@ -615,6 +619,30 @@ __device__ __forceinline__ void trace_fast(const Geometry &G, const tg_image_hea
                             fmaf(w.m[2] + (float)(kBatch - 2), w.pa[2], w.d[2]));
     if (!(bnd + margin < tstop)) break;
     guard -= kBatch;
+    if (!PJ) {
+      // backprojection: each segment's atomic is issued as soon as the step
+      // is known (fire-and-forget, so nothing is kept per step)
+      if (kDrift) {
+#pragma unroll
+        for (int s = 0; s < kBatch - 1; ++s) {
+          IDX o;
+          const float L = drift_step(w, cur, o);
+          accumulate<MODE, DET, IDX>(L, o, cin, cout, aout, yv, yq, qs, acc);
+        }
+        resync(w);
+        IDX o;
+        const float L = walk_step(w, cur, o);
+        accumulate<MODE, DET, IDX>(L, o, cin, cout, aout, yv, yq, qs, acc);
+      } else {
+#pragma unroll
+        for (int s = 0; s < kBatch; ++s) {
+          IDX o;
+          const float L = walk_step(w, cur, o);
+          accumulate<MODE, DET, IDX>(L, o, cin, cout, aout, yv, yq, qs, acc);
+        }
+      }
+      continue;
+    }
     float L[kBatch];
     IDX o[kBatch];
     if (kDrift) {
@@ -631,7 +659,7 @@ __device__ __forceinline__ void trace_fast(const Geometry &G, const tg_image_hea
     }
     if (CNT) {
       acc += (float)kBatch;
-    } else if (PJ) {
+    } else {
       float v[kBatch];
 #pragma unroll
       for (int s = 0; s < kBatch; ++s) v[s] = __ldg(cin + o[s]);
@@ -639,26 +667,6 @@ __device__ __forceinline__ void trace_fast(const Geometry &G, const tg_image_hea
 #pragma unroll
       for (int s = 1; s < kBatch; ++s) part = fmaf(L[s], v[s], part);
       acc += part;
-    } else {
-#pragma unroll
-      for (int s = 0; s < kBatch; ++s) {
-        if (!DET && TG_BPJ_PAIR) {
-          // neighbouring pixels (lanes l, l ^ 1) are often in the same voxel
-          // at the same step: the even lane adds both contributions
-          const unsigned active = __activemask();
-          const bool partner = (active >> (lane ^ 1)) & 1u;
-          const float v = L[s] * yv;
-          const IDX po = __shfl_xor_sync(active, o[s], 1);
-          const float pv = __shfl_xor_sync(active, v, 1);
-          if (partner && po == o[s]) {
-            if (!(lane & 1)) red_add_f32(cout + o[s], v + pv);
-          } else {
-            red_add_f32(cout + o[s], v);
-          }
-        } else {
-          accumulate<MODE, DET, IDX>(L[s], o[s], cin, cout, aout, yv, yq, qs, acc);
-        }
-      }
     }
   }
   // Remaining steps before tstop, one at a time.

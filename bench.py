@@ -244,7 +244,7 @@ def run_ours(args):
     # CPU baseline first (host threads only; no GPU context yet)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        v, dt, threads, rays = cpu_sample(threads=os.cpu_count())
+        v, dt, threads, rays = cpu_sample(threads=os.cpu_count(), repeats=2)
         cpu = cpu_baseline_entry(v, threads, "oracle float32 (C/OpenMP restatement of the reference kernel), "
                                              "%d of 360 views (%d rays), projection + backprojection, %.1f s"
                                  % (CPU_SAMPLE_VIEWS, rays, dt))

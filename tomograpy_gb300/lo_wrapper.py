@@ -71,6 +71,8 @@ class Siddon(LinearOperator):
         self.obstacle = obstacle
         self.deterministic = deterministic
         self._workspace = None
+        self._blocks = None
+        self._stream = None
         self.data_shape = (self.n1, self.n2, self.n_views)
         n_in = int(np.prod(self.cube_shape))
         n_out = int(np.prod(self.data_shape))
@@ -94,17 +96,85 @@ class Siddon(LinearOperator):
             return torch.zeros((F, n0, n1, n2), dtype=self.tdtype, device=self.device).permute(1, 2, 3, 0)
         return torch.zeros(self.cube_shape, dtype=self.tdtype, device=self.device)
 
+    # -- host <-> device pipelining ------------------------------------------
+    PIPE_BLOCKS = 8
+
+    def _row_blocks(self):
+        """Blocks of image rows (multiples of 32, the kernels' tile height) and
+        their view tables: a block of rows [a, b) is the image of views whose
+        CRPIX1 is shifted by a, so it is traced with exactly the same ray
+        directions, and its slice of the (N1, N2, T) stack is contiguous."""
+        if self._blocks is None:
+            step = -(-self.n1 // self.PIPE_BLOCKS)
+            step = max(32, -(-step // 32) * 32)
+            blocks = []
+            for a in range(0, self.n1, step):
+                hdrs = [dict(h, CRPIX1=float(h["CRPIX1"]) - a) for h in self.data_header]
+                blocks.append((a, min(self.n1, a + step), S.upload_views(hdrs, self.frames, self.device)))
+            self._blocks = blocks
+        return self._blocks
+
+    def _pipelined(self, host):
+        return (torch.is_tensor(host) and not host.is_cuda and host.is_pinned() and self.n1 >= 64
+                and self.tdtype == torch.float32 and host.dtype == torch.float32)
+
+    def _copy_stream(self):
+        if self._stream is None:
+            self._stream = torch.cuda.Stream(device=self.device)
+        return self._stream
+
+    def _project_to_host(self, xd, out):
+        """P x into pinned host memory: each block of image rows is copied out
+        on a second stream while the next block is traced."""
+        y = torch.zeros(self.data_shape, dtype=self.tdtype, device=self.device)
+        o = out.view(self.data_shape)
+        main, copy = torch.cuda.current_stream(self.device), self._copy_stream()
+        mode = "pjt" if self.four_d else "pj"
+        for a, b, views in self._row_blocks():
+            S.run_device(mode, y[a:b], xd, views, self.mh, self.n_views,
+                         None if self.mask is None else self.mask[a:b], self.obstacle)
+            copy.wait_stream(main)
+            with torch.cuda.stream(copy):
+                o[a:b].copy_(y[a:b], non_blocking=True)
+        main.wait_stream(copy)
+        copy.synchronize()
+        return out
+
+    def _backproject_from_host(self, yh, out):
+        """P^T y from pinned host memory: each block of image rows is sent on a
+        second stream while the previous block is backprojected."""
+        yh = yh.view(self.data_shape)
+        yd = torch.empty(self.data_shape, dtype=self.tdtype, device=self.device)
+        x = self.new_cube()
+        main, copy = torch.cuda.current_stream(self.device), self._copy_stream()
+        copy.wait_stream(main)
+        mode = "bpjt" if self.four_d else "bpj"
+        for a, b, views in self._row_blocks():
+            with torch.cuda.stream(copy):
+                yd[a:b].copy_(yh[a:b], non_blocking=True)
+            main.wait_stream(copy)
+            S.run_device(mode, yd[a:b], x, views, self.mh, self.n_views,
+                         None if self.mask is None else self.mask[a:b], self.obstacle)
+        yd.record_stream(copy)
+        return self._out(x, out)
+
     def project(self, x, out=None):
         """y = P x.  ``x``: cube (CUDA or host tensor / array).  Returns a CUDA
-        tensor, or fills ``out`` (device or host tensor) and returns it."""
+        tensor, or fills ``out`` (device or host tensor) and returns it; a
+        pinned host ``out`` is filled block by block while the GPU traces."""
         xd = self._dev(x, self.cube_shape)
+        if out is not None and self._pipelined(out):
+            return self._project_to_host(xd, out)
         y = torch.zeros(self.data_shape, dtype=self.tdtype, device=self.device)
         S.run_device("pjt" if self.four_d else "pj", y, xd, self.views_dev, self.mh, self.n_views, self.mask,
                      self.obstacle)
         return self._out(y, out)
 
     def backproject(self, y, out=None):
-        """x = P^T y.  ``y``: data stack (CUDA or host tensor / array)."""
+        """x = P^T y.  ``y``: data stack (CUDA or host tensor / array; a pinned
+        host stack is sent block by block while the GPU traces)."""
+        if self._pipelined(y) and not self.deterministic:
+            return self._backproject_from_host(y, out)
         yd = self._dev(y, self.data_shape)
         x = self.new_cube()
         if self.deterministic and self.tdtype == torch.float32:

@@ -235,7 +235,6 @@ def run_ours(args):
     import torch
     import torch.distributed as dist
 
-    import tomograpy_gb300 as tg
     from tomograpy_gb300 import lo_wrapper, siddon, synthetic
 
     rank, world, local = dist_env()

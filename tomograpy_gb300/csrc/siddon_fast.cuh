@@ -59,6 +59,12 @@ namespace tg {
 #ifndef TG_BPJ_MIN_BLOCKS
 #define TG_BPJ_MIN_BLOCKS 4
 #endif
+#ifndef TG_PJ_SHORT_BATCH
+#define TG_PJ_SHORT_BATCH 4
+#endif
+#ifndef TG_BPJ_SHORT_BATCH
+#define TG_BPJ_SHORT_BATCH 1
+#endif
 #ifndef TG_PJ_DRIFT
 #define TG_PJ_DRIFT 1
 #endif
@@ -669,8 +675,40 @@ __device__ __forceinline__ void trace_fast(const Geometry &G, const tg_image_hea
       acc += part;
     }
   }
-  // Remaining steps before tstop, one at a time.
+  // Remaining steps before tstop: short exact batches (same bound, no
+  // drift; the projection's gathers of a short batch are in flight
+  // together), then one at a time.
   float part = 0.f;
+  constexpr int kShort = is_backprojection(MODE) ? TG_BPJ_SHORT_BATCH : TG_PJ_SHORT_BATCH;
+  while (kShort > 1 && guard >= kShort) {
+    const float bnd = min3f(fmaf(w.m[0] + (float)(kShort - 2), w.pa[0], w.d[0]),
+                            fmaf(w.m[1] + (float)(kShort - 2), w.pa[1], w.d[1]),
+                            fmaf(w.m[2] + (float)(kShort - 2), w.pa[2], w.d[2]));
+    if (!(bnd < tstop)) break;
+    guard -= kShort;
+    if (!PJ) {
+#pragma unroll
+      for (int s = 0; s < kShort; ++s) {
+        IDX o;
+        const float L = walk_step(w, cur, o);
+        accumulate<MODE, DET, IDX>(L, o, cin, cout, aout, yv, yq, qs, part);
+      }
+    } else {
+      float L[kShort > 1 ? kShort : 1], v[kShort > 1 ? kShort : 1];
+#pragma unroll
+      for (int s = 0; s < kShort; ++s) {
+        IDX o;
+        L[s] = walk_step(w, cur, o);
+        v[s] = CNT ? 1.f : __ldg(cin + o);
+      }
+      if (CNT) {
+        part += (float)kShort;
+      } else {
+#pragma unroll
+        for (int s = 0; s < kShort; ++s) part = fmaf(L[s], v[s], part);
+      }
+    }
+  }
   while (cur < tstop && guard > 0) {
     --guard;
     IDX o;

@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the uneven multi-job batch measurement")
     ap.add_argument("--no-served", action="store_true", help="skip the serving-stream measurement")
     ap.add_argument("--no-4d", action="store_true", help="skip the time-dependent (4-D) measurement")
+    ap.add_argument("--no-lbfgs", action="store_true", help="skip the differentiable-reconstruction measurement")
     ap.add_argument("--served-jobs", type=int, default=60,
                     help="requests of the serving stream sample (Poisson, 20 jobs/s)")
     ap.add_argument("--profile-case", action="store_true",
@@ -316,6 +317,7 @@ def run_ours(args):
     for k in kern.values():
         k["gbs"] = k["bytes"] / (k["ms"] / 1000.0) / 1e9
         k["frac"] = k["gbs"] / peak
+    det_ms = deterministic_bpj_ms(y, c, views, mh, T, n, flush, e)
     dom = max(kern, key=lambda k: kern[k]["ms"])
     traffic = ncu_traffic(dom)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": kern[dom]["gbs"], "peak": peak, "unit": "GB/s",
@@ -345,7 +347,9 @@ def run_ours(args):
                "h2d_bytes_per_step": vol + img, "d2h_bytes_per_step": img + vol,
                "path": "lo_wrapper.siddon_lo project/backproject, pinned host tensors"}
 
-    batched = served = four_d = None
+    batched = served = four_d = lbfgs = None
+    if rank == 0 and not args.no_lbfgs:
+        lbfgs = measure_lbfgs(dev)
     if rank == 0 and not args.no_4d:
         four_d = measure_4d(dev)
     if rank == 0 and not args.no_batched:
@@ -364,12 +368,14 @@ def run_ours(args):
                        "intersections_per_step": inter, "hit_rays_per_step": hit,
                        "l2": "flushed between steps (256 MiB write, untimed)", "parallelism": "replicas"},
             "intersections_per_s": world * inter * 2 / (ms / 1000.0),
-            "kernels": {k: {"ms": v["ms"], "GB_s": v["gbs"], "frac": v["frac"]} for k, v in kern.items()},
+            "kernels": dict({k: {"ms": v["ms"], "GB_s": v["gbs"], "frac": v["frac"]} for k, v in kern.items()},
+                            siddon_bpj_f32_deterministic={"ms": det_ms}),
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": 2 * args.steps,
             "clocks": clk,
+            "lbfgs": lbfgs,
             "four_d": four_d,
             "batched": batched,
             "served": served,
@@ -377,6 +383,52 @@ def run_ours(args):
         print(json.dumps(out), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def deterministic_bpj_ms(y, c, views, mh, T, n, flush, e, reps=3):
+    """Mean time of the deterministic (int64 fixed-point) backprojection of the
+    workload's data stack (outside the headline step)."""
+    import torch
+
+    from tomograpy_gb300 import _lib, siddon
+    need = _lib.load().tg_deterministic_workspace_bytes(_lib.i64([n, n, n, 1]))
+    ws = torch.empty(need, dtype=torch.uint8, device=c.device)
+    ts = []
+    for r in range(reps + 1):
+        flush.fill_(1.0)
+        c.zero_()
+        e[0].record()
+        siddon.run_device("bpj", y, c, views, mh, T, obstacle="sun", deterministic=True, workspace=ws)
+        e[1].record()
+        torch.cuda.synchronize()
+        if r:
+            ts.append(e[0].elapsed_time(e[1]))
+    return statistics.mean(ts)
+
+
+def measure_lbfgs(dev, iters=10):
+    """Differentiable reconstruction on the benchmark geometry: L-BFGS on
+    0.5 |P x - y|^2 / |y|^2 + 1e-3 TV_eps(x) with x = s softplus(z), the
+    projector as a torch.autograd.Function whose backward is the
+    backprojector; y = P(phantom) with Poisson noise at 1e4 counts peak."""
+    import numpy as np
+    import torch
+
+    from tomograpy_gb300 import autograd, lo_wrapper, synthetic
+    ch, vh = synthetic.make_geometry(WORKLOAD)
+    op = lo_wrapper.siddon_lo(vh, ch, obstacle="sun", dtype=np.float32, device=dev)
+    x = torch.from_numpy(synthetic.phantom(ch, seed=0) / np.float32(1e8)).to(dev)
+    y = op.project(x)
+    y = torch.from_numpy(synthetic.poisson_noise(y.cpu().numpy())).to(dev)
+    autograd.reconstruct_lbfgs(op, y, iters=1)          # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    xr, losses = autograd.reconstruct_lbfgs(op, y, iters=iters)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    return {"workload": "256^3 x 360 x 512^2, sun, L-BFGS (strong Wolfe) with TV 1e-3 and softplus positivity",
+            "iterations": iters, "loss_evaluations": len(losses), "seconds": dt,
+            "s_per_evaluation": dt / max(1, len(losses)), "loss_first": losses[0], "loss_last": losses[-1]}
 
 
 def measure_4d(dev, reps=5, cg_iters=30):

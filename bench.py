@@ -29,6 +29,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -96,7 +97,7 @@ class Clocks:
 
     def __init__(self, uuid=None):
         self.uuid = uuid
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_%d.csv" % os.getpid())
+        self.path = os.path.join(tempfile.gettempdir(), "tomograpy_gb300_clocks_%d.csv" % os.getpid())
         self.proc = None
 
     def start(self):

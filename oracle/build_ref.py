@@ -89,6 +89,11 @@ def _compile(args):
     return out
 
 
+def reference_present(reference=DEFAULT_REFERENCE):
+    """True where the reference checkout is available (not on the GPU host)."""
+    return os.path.isdir(os.path.join(reference, "tomograpy"))
+
+
 def build(reference=DEFAULT_REFERENCE, quiet=False):
     """Compile all 16 reference variants into oracle/_ref/. Returns the list of .so paths."""
     import numpy

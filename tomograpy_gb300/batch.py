@@ -12,7 +12,7 @@ is ~130 CTAs for 152 SMs) and pays one launch per job per operation.  Here:
   per-job float64 inner products (``tg_segmented_dot_f32``) and per-job
   scalars stay on the device (``tg_cg_update_x`` / ``_p``), so an iteration
   is a fixed sequence of launches, captured once in a CUDA graph and replayed;
-* :func:`autotune` picks the CTA tile height (rows per warp) by timing the
+* :meth:`PackedJobs.autotune` picks the CTA tile height (rows per warp) by timing the
   packed projector + backprojector on the actual job set, cached per job-set
   signature;
 * :func:`sequential_cg` is the plain per-job loop the batched form is

@@ -338,7 +338,11 @@ static tg_status build_packed_plan(const tg_job *jobs, int32_t n_jobs, int32_t r
     tg_status st = make_geometry(geoms[j], &J.map_header, J.views, J.n_views, J.n1, J.n2, J.data_strides,
                                  J.map_shape, J.map_strides, J.mask, (tg_dtype)J.mask_dtype, J.mask_strides,
                                  four_d != 0, &i64);
-    if (st != TG_OK) return fail(st, "job %d: %s", j, g_err);
+    if (st != TG_OK) {
+      char why[sizeof(g_err)];
+      std::memcpy(why, g_err, sizeof(why));  // fail() writes g_err: format from a copy
+      return fail(st, "job %d: %s", j, why);
+    }
     if (J.n_views > 0 && J.n1 > 0 && J.n2 > 0 && (!J.data || !J.map))
       return fail(TG_EINVAL, "job %d: data or map pointer is NULL", j);
     idx64 = idx64 || i64;

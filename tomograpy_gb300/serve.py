@@ -5,10 +5,11 @@ keeps every admitted job's data stack and CG vectors resident on the GPU and,
 at each scheduler step, advances *all* in-flight jobs by one CG iteration on
 (P^T P + lam I) x = P^T y with packed launches (``tg_packed_projector``, one
 launch per direction for all jobs, plus segmented vector kernels).  Jobs join
-as soon as device memory allows (first-fit arenas; admission is by bytes,
-not by a slot count) and leave when they converge (relative residual <= tol)
-or reach their iteration budget, so requests that arrive while others are on
-the GPU overlap with them.
+as soon as device memory allows (first-fit arenas; admission is by bytes and
+in-flight rays, not by a slot count; shortest job first with aging) and leave
+when they converge (relative residual <= tol) or reach their iteration
+budget, so requests that arrive while others are on the GPU overlap with
+them.
 
 Reported per run: p50 / p99 time-to-solution (arrival to result on the host),
 jobs/s and CG-iterations/s.  :func:`fifo_plain` is the baseline: the same
@@ -348,24 +349,31 @@ class Server:
         return sum(job.nd for job in self.inflight)
 
     def _admit(self, queue, now):
-        """Admit queued requests: in arrival order while the in-flight rays stay
-        under ``max_rays`` (one step is then a few tens of waves of the GPU, so
-        a newcomer waits at most one such step) and memory allows; a request
-        that does not fit is skipped by later, smaller ones (backfill) unless
-        it has waited ``max_wait`` seconds, and it is always admitted into an
-        empty server."""
+        """Admit queued requests while the in-flight rays stay under
+        ``max_rays`` (one step is then a few tens of waves of the GPU) and
+        memory allows.  Candidates are taken shortest job first (fewest rays:
+        a small request is not held behind a large one), except that a
+        request waiting longer than ``max_wait`` seconds goes first and, if it
+        does not fit, stops further admissions until the server drains enough
+        for it; an empty server always admits its first candidate."""
+        if not queue:
+            return
         rays = self._rays_inflight()
-        k = 0
-        while k < len(queue):
+        order = sorted(range(len(queue)),
+                       key=lambda k: (now - queue[k].arrival < self.max_wait, int(np.prod(queue[k].job.data_shape)),
+                                      queue[k].arrival))
+        admitted = set()
+        for k in order:
             req = queue[k]
             need = int(np.prod(req.job.data_shape))
             if (not self.inflight or rays + need <= self.max_rays) and self.try_admit(req):
-                queue.pop(k)
+                admitted.add(k)
                 rays += need
                 continue
-            if k == 0 and now - req.arrival >= self.max_wait:
-                break  # the head has waited long enough: let the server drain for it
-            k += 1
+            if now - req.arrival >= self.max_wait:
+                break  # an old request is waiting: let the server drain for it
+        if admitted:
+            queue[:] = [r for k, r in enumerate(queue) if k not in admitted]
 
     def run(self, requests):
         """Serve ``requests`` (sorted by arrival time, seconds from now)."""

@@ -59,6 +59,9 @@ def parse():
     ap.add_argument("--no-lbfgs", action="store_true", help="skip the differentiable-reconstruction measurement")
     ap.add_argument("--served-jobs", type=int, default=60,
                     help="requests of the serving stream sample (Poisson, 20 jobs/s)")
+    ap.add_argument("--profile-packed", action="store_true",
+                    help="one packed projection + backprojection of the 32-job uneven batch (the case of the "
+                         "packed-kernel ncu summary in profiles/)")
     ap.add_argument("--profile-case", action="store_true",
                     help="one projection + one backprojection on the workload's geometry restricted to every "
                          "10th view (36 views): the case the ncu summaries in profiles/ are captured on")
@@ -588,10 +591,29 @@ def run_profile_case():
     print(json.dumps({"profile_case": WORKLOAD, "views": T, "y_sum": float(y.sum()), "c_sum": float(c.sum())}))
 
 
+def run_profile_packed():
+    import torch
+
+    from tomograpy_gb300 import batch, synthetic
+    jobs = [synthetic.make_job(sp, seed=k) for k, sp in enumerate(synthetic.uneven_specs(32, seed=0))]
+    pack = batch.PackedJobs(jobs, obstacle="sun", rows_per_warp=4)
+    x = pack.new_cube()
+    for k, j in enumerate(jobs):
+        pack.cube_view(x, k).copy_(torch.from_numpy(j.phantom))
+    pack.project(x)
+    z = pack.backproject(pack.new_cube())
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_packed": 32, "rays": int(pack.data.numel()), "y_sum": float(pack.data.sum()),
+                      "c_sum": float(z.sum())}))
+
+
 def main():
     args = parse()
     if args.profile_case:
         run_profile_case()
+        return
+    if args.profile_packed:
+        run_profile_packed()
         return
     if args.impl == "reference":
         run_reference(args)

@@ -9,23 +9,25 @@
 //
 // Arithmetic (the reference does everything in its C type,
 // tomograpy/C_siddon.c.template:530-580,811-912):
-//  * per-ray set-up in double precision: direction (cos l * A_row + sin l *
-//    R[:, 2] with per-row A_row = R . (cos g, sin g, 0) tabulated per CTA),
-//    entry parameter amin exactly as the reference computes it, entry voxel by
-//    a floor division; single precision only classifies the ray (miss / clear
-//    entry face) and the full double-precision reference set-up
-//    (siddon_geom.cuh) runs when that classification is within its error
-//    bound;
+//  * per-ray set-up in double-float (pairs of floats, FMA-based error-free
+//    products) from per-CTA tables computed in double precision: direction
+//    cos l * (A_row + tan l * R[:, 2]) with A_row = R . (cos g, sin g, 0),
+//    entry parameter, entry point (the two ~d-sized terms cancel to ~1e-11),
+//    entry voxel by a floor division against the exact plane positions, and
+//    the crossing spacing CDELT / |w|.  Single precision only classifies the
+//    ray (miss / clear entry face); the full double-precision reference
+//    set-up (siddon_geom.cuh) runs when that classification is within its
+//    error bound;
 //  * the voxel walk in single precision, measured from the chord's midpoint:
-//    the k-th plane crossing of family a is t = d_a + k * |p_a| (one FMA, no
-//    running sum) with k counted from the crossing nearest the midpoint and
-//    d_a, |p_a| derived from double-float values, so crossing positions carry
-//    no accumulated drift, their rounding scales with the distance from the
-//    midpoint, and the catastrophic cancellation of the reference's float
-//    path (D[k] = next*p + a1 - amin with a1, amin ~ 215) never occurs.  Steps run
-//    in batches of kBatch that are proven, by one bound, to start before the
-//    stop parameter, so a batch needs no per-step test and its kBatch cube
-//    gathers are issued together;
+//    the k-th plane crossing of family a is t = d_a + k * |p_a| (one FMA)
+//    with k counted from the crossing nearest the midpoint, so crossing
+//    positions carry no accumulated drift, their rounding scales with the
+//    distance from the midpoint, and the catastrophic cancellation of the
+//    reference's float path (D[k] = next*p + a1 - amin with a1, amin ~ 215)
+//    never occurs.  Steps run in batches that are proven, by one bound, to
+//    start before the stop parameter, so a batch needs no per-step test and
+//    its gathers / atomics are issued together; inside a batch the crossings
+//    advance by running sums (one add) and are recomputed exactly after it;
 //  * the "sun" obstacle: the reference tests |M + ac u|^2 > 1 at every voxel
 //    entry (:575).  Here the walk runs unchecked up to the sphere-entry
 //    parameter minus an error bound; from there on every voxel entry is tested
@@ -72,7 +74,7 @@ namespace tg {
 #define TG_BPJ_DRIFT 1
 #endif
 __host__ __device__ constexpr bool is_backprojection(int mode) { return mode == TG_BPJ || mode == TG_BPJT; }
-// running-sum crossings inside projection batches (drift_step)
+// running-sum crossings inside batches (drift_step), per direction
 __host__ __device__ constexpr bool drift_batches(int mode) {
   return is_backprojection(mode) ? TG_BPJ_DRIFT : TG_PJ_DRIFT;
 }

@@ -81,9 +81,12 @@ def _stream():
 
 
 class Job:
-    """One reconstruction: cube header, view headers, optional data (N1, N2, T)."""
+    """One reconstruction: cube header, view headers, optional data (N1, N2, T).
 
-    def __init__(self, cube_header, view_headers, data=None, obstacle="sun"):
+    ``frames`` (one cube frame index per view) makes it a time-dependent job
+    with a (n0, n1, n2, F) cube, F = max(frames) + 1."""
+
+    def __init__(self, cube_header, view_headers, data=None, obstacle="sun", frames=None):
         self.cube_header = dict(cube_header)
         if "MMAX1" not in self.cube_header:
             S.H.map_borders(self.cube_header)
@@ -92,6 +95,12 @@ class Job:
             if "R1_1" not in h:
                 S.H.header_rotation_matrix(h)
         self.cube_shape = tuple(int(self.cube_header["NAXIS%d" % (k + 1)]) for k in range(3))
+        self.frames = None
+        if frames is not None:
+            self.frames = np.asarray(frames, dtype=np.int64)
+            if self.frames.shape != (len(self.view_headers),) or self.frames.min() < 0:
+                raise ValueError("frames must give one non-negative frame index per view")
+            self.cube_shape = self.cube_shape + (int(self.frames.max()) + 1,)
         h0 = self.view_headers[0]
         self.data_shape = (int(h0["NAXIS1"]), int(h0["NAXIS2"]), len(self.view_headers))
         self.data = data
@@ -116,7 +125,10 @@ class PackedJobs:
         dev = self.device
         # per-job element ranges [start, end) of the flat cube buffers
         self.cube_seg_dev = torch.from_numpy(np.stack([self.cube_off[:-1], self.cube_off[1:]], 1).reshape(-1).copy()).to(dev)
-        self.views = [S.upload_views(j.view_headers, None, dev) for j in self.jobs]
+        self.four_d = any(j.frames is not None for j in self.jobs)
+        if self.four_d and not all(j.frames is not None for j in self.jobs):
+            raise ValueError("a pack holds either 3-D or time-dependent (4-D) jobs, not both")
+        self.views = [S.upload_views(j.view_headers, j.frames, dev) for j in self.jobs]
         self.mhs = [S.pack_map_header(j.cube_header) for j in self.jobs]
         self.data = torch.zeros(int(self.data_off[-1]), dtype=torch.float32, device=dev)
         self._plans = {}
@@ -130,8 +142,13 @@ class PackedJobs:
         return seg.view(T, n1, n2).permute(1, 2, 0)
 
     def cube_view(self, flat, k):
+        """Job k's cube in a flat cube buffer; 4-D cubes are stored frame-major
+        (F, n0, n1, n2) and viewed as (n0, n1, n2, F)."""
         seg = flat[int(self.cube_off[k]):int(self.cube_off[k + 1])]
-        return seg.view(*self.jobs[k].cube_shape)
+        shape = self.jobs[k].cube_shape
+        if len(shape) == 4:
+            return seg.view(shape[3], *shape[:3]).permute(1, 2, 3, 0)
+        return seg.view(*shape)
 
     def new_cube(self):
         return torch.zeros(int(self.cube_off[-1]), dtype=torch.float32, device=self.device)
@@ -156,8 +173,8 @@ class PackedJobs:
                 J.data_strides[a] = d.stride()[a]
                 J.map_shape[a] = c.shape[a]
                 J.map_strides[a] = c.stride()[a]
-            J.map_shape[3] = 1
-            J.map_strides[3] = 0
+            J.map_shape[3] = c.shape[3] if c.dim() == 4 else 1
+            J.map_strides[3] = c.stride()[3] if c.dim() == 4 else 0
             J.mask = None
             J.mask_dtype = _lib.TG_U8
             J.data = d.data_ptr()
@@ -165,7 +182,7 @@ class PackedJobs:
         nbytes = self.L.tg_packed_plan_bytes(self.n)
         buf = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
         info = TgPackedInfo()
-        _lib.check(self.L.tg_packed_plan(arr, self.n, rpw, 0, _ptr(buf), nbytes, ctypes.byref(info)))
+        _lib.check(self.L.tg_packed_plan(arr, self.n, rpw, int(self.four_d), _ptr(buf), nbytes, ctypes.byref(info)))
         self._plans[key] = (buf, info, arr)
         return self._plans[key]
 
@@ -173,7 +190,7 @@ class PackedJobs:
         """self.data = P cube (all jobs, one launch; data zeroed first)."""
         buf, info, _ = self.plan(cube_flat, rows_per_warp)
         self.data.zero_()
-        _lib.check(self.L.tg_packed_projector(_ptr(buf), ctypes.byref(info), _lib.TG_PJ,
+        _lib.check(self.L.tg_packed_projector(_ptr(buf), ctypes.byref(info), _lib.TG_PJT if self.four_d else _lib.TG_PJ,
                                               _lib.OBSTACLES[self.obstacle], _stream()))
         return self.data
 
@@ -181,7 +198,8 @@ class PackedJobs:
         """cube_flat = P^T self.data (all jobs, one launch; cube zeroed first)."""
         buf, info, _ = self.plan(cube_flat, rows_per_warp)
         cube_flat.zero_()
-        _lib.check(self.L.tg_packed_projector(_ptr(buf), ctypes.byref(info), _lib.TG_BPJ,
+        _lib.check(self.L.tg_packed_projector(_ptr(buf), ctypes.byref(info),
+                                              _lib.TG_BPJT if self.four_d else _lib.TG_BPJ,
                                               _lib.OBSTACLES[self.obstacle], _stream()))
         return cube_flat
 

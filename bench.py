@@ -491,6 +491,7 @@ def measure_4d(dev, reps=5, cg_iters=30):
                    "relative_residual": res.residuals[-1]}}
 
 
+SERVE_BUDGET = 48 << 30   # device memory the serving measurement may keep resident
 SMALL_MIX = dict(edges=(16, 24, 32, 48), sides=(32, 48, 64), views=(8, 32))
 
 
@@ -552,11 +553,11 @@ def measure_served(dev, n_jobs=60, rate=20.0, seed=0, mix=None, large=0.1):
     # warm-up (untimed): the first launches of every kernel variant and the
     # first pinned allocations of a process would otherwise land in the stream
     warm = serve.poisson_requests(specs[:8], rate=1e6, seed=seed, max_iters=3, tol=1e-4, device=dev)
-    serve.Server(device=dev).run(warm)
+    serve.Server(budget_bytes=8 << 30, device=dev).run(warm)
     serve.fifo_plain(serve.poisson_requests(specs[:8], rate=1e6, seed=seed, max_iters=3, tol=1e-4, device=dev),
                      device=dev)
     reqs = serve.poisson_requests(specs, rate=rate, seed=seed, max_iters=20, tol=1e-4, device=dev)
-    srv = serve.Server(device=dev)
+    srv = serve.Server(budget_bytes=SERVE_BUDGET, device=dev)
     s = srv.run(reqs)
     reqs2 = serve.poisson_requests(specs, rate=rate, seed=seed, max_iters=20, tol=1e-4, device=dev)
     f = serve.fifo_plain(reqs2, device=dev)
@@ -567,7 +568,7 @@ def measure_served(dev, n_jobs=60, rate=20.0, seed=0, mix=None, large=0.1):
     return {"workload": "serving stream: %d Poisson requests at %.0f jobs/s, %s + %d%% 256^3 x 360 x 512^2, "
                         "20 CG iterations or residual 1e-4" % (n_jobs, rate, sizes, round(100 * large)),
             "served": s, "fifo_plain": f, "cg_it_per_s_ratio": s["cg_it_per_s"] / f["cg_it_per_s"],
-            "max_inflight": srv.max_inflight, "max_rel_diff_vs_plain": diff,
+            "max_inflight": srv.max_inflight, "max_rel_diff_vs_plain": diff, "budget_bytes": SERVE_BUDGET,
             "server_host_s": srv.host_s, "server_rebuilds": srv.rebuilds}
 
 

@@ -405,6 +405,9 @@ class Server:
             t2 = time.perf_counter()
             self.host_s["admit"] += t1 - t0
             self.host_s["collect"] += t2 - t1
+            if not self.inflight and queue and self._limbo:
+                self._read_residuals(keep_queued=0)  # release the slots of retired jobs
+                self._admit(queue, now)
             if not self.inflight:
                 if queue:
                     raise RuntimeError("request %d does not fit the memory budget" % queue[0].id)

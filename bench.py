@@ -350,6 +350,7 @@ def run_ours(args):
         e2e = {"value": world * rays / (e2e_ms / 1000.0), "unit": UNIT, "ms_per_step": e2e_ms,
                "h2d_bytes_per_step": vol + img, "d2h_bytes_per_step": img + vol,
                "path": "lo_wrapper.siddon_lo project/backproject, pinned host tensors"}
+        e2e["drop_in_numpy"] = drop_in_numpy_rate(ch, vh, x.cpu().numpy(), rays, reps=2)
 
     batched = served = four_d = lbfgs = None
     if rank == 0 and not args.no_lbfgs:
@@ -387,6 +388,31 @@ def run_ours(args):
         print(json.dumps(out), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def drop_in_numpy_rate(ch, vh, x, rays, reps=2):
+    """The reference's own call pattern: tomograpy.projector(data, cube) then
+    tomograpy.backprojector(data, cube) on NumPy arrays with headers (each
+    call stages its arrays through the GPU and writes back in place)."""
+    import numpy as np
+
+    import tomograpy_gb300 as tgp
+    from tomograpy_gb300.infoarray import InfoArray
+    N, T = int(vh[0]["NAXIS1"]), len(vh)
+    data = InfoArray(shape=(N, N, T), header=[dict(h) for h in vh], dtype=np.float32)
+    cube = InfoArray(data=x, header=dict(ch))
+    back = InfoArray(shape=x.shape, header=dict(ch), dtype=np.float32)
+    tgp.projector(data, cube, obstacle="sun")
+    tgp.backprojector(data, back, obstacle="sun")
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        data[...] = 0
+        back[...] = 0
+        tgp.projector(data, cube, obstacle="sun")
+        tgp.backprojector(data, back, obstacle="sun")
+    ms = 1000.0 * (time.perf_counter() - t0) / reps
+    return {"value": rays / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms,
+            "path": "tomograpy_gb300.projector / backprojector on NumPy arrays (pageable host memory)"}
 
 
 def deterministic_bpj_ms(y, c, views, mh, T, n, flush, e, reps=3):

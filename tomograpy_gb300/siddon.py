@@ -290,11 +290,17 @@ def _run(mode, data, cube, mask, obstacle, view=None, ray=None, frames=None, det
     d_t = torch.from_numpy(np.ascontiguousarray(d_np)).to(dev)
     c_t = torch.from_numpy(np.ascontiguousarray(c_np)).to(dev)
     run_device(mode, d_t, c_t, views_dev, mh, T, _mask_to_device(mask, dev), obstacle, view, ray, deterministic)
-    if mode in ("pj", "pjt"):
-        d_np[...] = d_t.cpu().numpy()
-        return data
-    c_np[...] = c_t.cpu().numpy()
-    return cube
+    _write_back(d_np if mode in ("pj", "pjt") else c_np, d_t if mode in ("pj", "pjt") else c_t)
+    return data if mode in ("pj", "pjt") else cube
+
+
+def _write_back(dst, src):
+    """Device result -> the caller's NumPy array, in place (one copy when the
+    array is C-contiguous in the result's dtype)."""
+    if dst.flags.c_contiguous and dst.dtype == np.dtype(str(src.dtype).replace("torch.", "")):
+        torch.from_numpy(dst).copy_(src.reshape(dst.shape))
+    else:
+        dst[...] = src.cpu().numpy()
 
 
 def projector(data, cube, mask=None, obstacle=None, nthread=0, **kw):

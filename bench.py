@@ -350,19 +350,21 @@ def run_ours(args):
         e2e = {"value": world * rays / (e2e_ms / 1000.0), "unit": UNIT, "ms_per_step": e2e_ms,
                "h2d_bytes_per_step": vol + img, "d2h_bytes_per_step": img + vol,
                "path": "lo_wrapper.siddon_lo project/backproject, pinned host tensors"}
-        e2e["drop_in_numpy"] = drop_in_numpy_rate(ch, vh, x.cpu().numpy(), rays, reps=2)
+        e2e["drop_in_numpy"] = guarded(drop_in_numpy_rate, ch, vh, x.cpu().numpy(), rays, reps=2)
 
     batched = served = four_d = lbfgs = None
     if rank == 0 and not args.no_lbfgs:
-        lbfgs = measure_lbfgs(dev)
+        lbfgs = guarded(measure_lbfgs, dev)
     if rank == 0 and not args.no_4d:
-        four_d = measure_4d(dev)
+        four_d = guarded(measure_4d, dev)
     if rank == 0 and not args.no_batched:
-        batched = measure_batched(dev)
-        batched["small_jobs"] = measure_batched(dev, n_jobs=256, mix=SMALL_MIX)
+        batched = guarded(measure_batched, dev)
+        if "error" not in batched:
+            batched["small_jobs"] = guarded(measure_batched, dev, n_jobs=256, mix=SMALL_MIX)
     if rank == 0 and not args.no_served:
-        served = measure_served(dev, args.served_jobs)
-        served["small_jobs"] = measure_served(dev, 500, rate=1000.0, mix=SMALL_MIX, large=0.0)
+        served = guarded(measure_served, dev, args.served_jobs)
+        if "error" not in served:
+            served["small_jobs"] = guarded(measure_served, dev, 500, rate=1000.0, mix=SMALL_MIX, large=0.0)
 
     if rank == 0:
         out = {
@@ -388,6 +390,18 @@ def run_ours(args):
         print(json.dumps(out), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def guarded(fn, *a, **kw):
+    """Run a secondary measurement; a failure is reported in its entry (the
+    headline line is printed whatever happens to the secondary ones)."""
+    try:
+        return fn(*a, **kw)
+    except Exception as e:  # noqa: BLE001 - reported, not hidden
+        import torch
+        torch.cuda.synchronize()
+        print("bench: %s failed: %r" % (fn.__name__, e), file=sys.stderr)
+        return {"error": "%s: %s" % (type(e).__name__, e)}
 
 
 def drop_in_numpy_rate(ch, vh, x, rays, reps=2):

@@ -398,8 +398,6 @@ def guarded(fn, *a, **kw):
     try:
         return fn(*a, **kw)
     except Exception as e:  # noqa: BLE001 - reported, not hidden
-        import torch
-        torch.cuda.synchronize()
         print("bench: %s failed: %r" % (fn.__name__, e), file=sys.stderr)
         return {"error": "%s: %s" % (type(e).__name__, e)}
 

@@ -364,7 +364,7 @@ def run_ours(args):
     if rank == 0 and not args.no_served:
         served = guarded(measure_served, dev, args.served_jobs)
         if "error" not in served:
-            served["small_jobs"] = guarded(measure_served, dev, 500, rate=1000.0, mix=SMALL_MIX, large=0.0)
+            served["small_jobs"] = guarded(measure_served, dev, 500, rate=4000.0, mix=SMALL_MIX, large=0.0)
 
     if rank == 0:
         out = {

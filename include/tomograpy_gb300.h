@@ -157,7 +157,10 @@ tg_status tg_conic_full_backprojector_deterministic(
  * cube to (32 MiB - 256 B) / 8 = 4,194,272 voxels (n0*n1*n2, times the frame
  * count for TG_BPJT); larger cubes are rejected with TG_ENOMEM.  The first
  * call on a device looks up the scratch address (cudaGetSymbolAddress) with
- * that device current, so make it before any stream capture.  Every call
+ * that device current and keeps it for the life of the process, so make that
+ * first call before any stream capture, and do not call this entry point on a
+ * device after a cudaDeviceReset() of it (the kept address would then name
+ * freed memory).  Every call
  * shares the scratch and clears it first: calls that overlap on the GPU
  * (different streams or host threads) race. */
 size_t tg_noalloc_scratch_bytes(void);

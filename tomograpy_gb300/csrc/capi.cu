@@ -50,7 +50,8 @@ tg_status make_geometry(tg::Geometry &G, const tg_map_header *mh, const tg_image
   for (int k = 0; k < 3; ++k)
     if (map_shape[k] < 1 || map_shape[k] > (1 << 20))
       return fail(TG_EINVAL, "cube axis %d has %lld voxels", k, (long long)map_shape[k]);
-  if (four_d && map_shape[3] < 1) return fail(TG_EINVAL, "4-D cube needs at least one frame");
+  if (four_d && (map_shape[3] < 1 || map_shape[3] > 2147483647LL))
+    return fail(TG_EINVAL, "4-D cube has %lld frames (1 to 2^31 - 1 allowed)", (long long)map_shape[3]);
   if (mask) {
     if (!ks) return fail(TG_EINVAL, "mask strides are NULL");
     if (mask_dtype != TG_U8 && mask_dtype != TG_F32 && mask_dtype != TG_F64)
@@ -224,10 +225,15 @@ tg_status tg_intersection_parameters(const tg_map_header *map_header, const tg_i
 
 size_t tg_deterministic_workspace_bytes(const int64_t map_shape[4]) {
   if (!map_shape) return 0;
+  // checked arithmetic: a shape whose accumulator does not fit in size_t
+  // needs SIZE_MAX bytes, which no workspace (or the built-in scratch) holds
   size_t vox = 1;
-  for (int k = 0; k < 4; ++k) vox *= (size_t)(map_shape[k] > 0 ? map_shape[k] : 1);
-  size_t bytes = 256 + vox * 8;
-  return (bytes + 255) & ~(size_t)255;
+  for (int k = 0; k < 4; ++k)
+    if (__builtin_mul_overflow(vox, (size_t)(map_shape[k] > 0 ? map_shape[k] : 1), &vox)) return SIZE_MAX;
+  size_t bytes;
+  if (__builtin_mul_overflow(vox, (size_t)8, &bytes) || __builtin_add_overflow(bytes, (size_t)(256 + 255), &bytes))
+    return SIZE_MAX;
+  return bytes & ~(size_t)255;
 }
 
 tg_status tg_conic_full_backprojector_deterministic(
@@ -243,9 +249,9 @@ tg_status tg_conic_full_backprojector_deterministic(
   const bool four_d = (mode == TG_BPJT);
   int64_t shape4[4] = {map_shape ? map_shape[0] : 0, map_shape ? map_shape[1] : 0, map_shape ? map_shape[2] : 0,
                        four_d && map_shape ? map_shape[3] : 1};
-  if (workspace_bytes < tg_deterministic_workspace_bytes(shape4))
-    return fail(TG_ENOMEM, "workspace has %zu bytes, needs %zu", workspace_bytes,
-                tg_deterministic_workspace_bytes(shape4));
+  const size_t need = tg_deterministic_workspace_bytes(shape4);
+  if (need == SIZE_MAX) return fail(TG_EINVAL, "cube too large for a 64-bit accumulator");
+  if (workspace_bytes < need) return fail(TG_ENOMEM, "workspace has %zu bytes, needs %zu", workspace_bytes, need);
   tg::Geometry G;
   bool idx64 = false;
   tg_status st = make_geometry(G, map_header, views, n_views, n1, n2, data_strides, map_shape, map_strides, mask,
@@ -433,7 +439,7 @@ tg_status tg_conic_full_backprojector_deterministic_noalloc(
                 "cube of %lld x %lld x %lld x %lld voxels needs %zu bytes of scratch; the built-in scratch holds "
                 "%zu bytes (%zu voxels): use tg_conic_full_backprojector_deterministic with a workspace",
                 (long long)shape4[0], (long long)shape4[1], (long long)shape4[2], (long long)shape4[3], need,
-                tg::noalloc_scratch_bytes(), (tg::noalloc_scratch_bytes() - 256) / 8);
+                tg::noalloc_scratch_bytes(), tg::noalloc_scratch_voxels());
   void *scratch = nullptr;
   cudaError_t e = tg::noalloc_scratch(&scratch);
   if (e != cudaSuccess) return launch_status(e, "scratch address lookup");

@@ -12,8 +12,11 @@
 // (32 MiB): every GPU that loads the library holds it until the process
 // exits.  Host code cannot use the array's name as a device address, so the
 // first call on each device looks the address up with cudaGetSymbolAddress
-// (with that device current) and caches it; that first call should therefore
-// come before any stream capture.  All calls share the one array: the scratch
+// (with that device current) and caches it for the life of the process; that
+// first call should therefore come before any stream capture, and no call may
+// follow a cudaDeviceReset() of a device the entry point has already been used
+// on (the reset unloads the library's device code, so the cached address would
+// name freed memory).  All calls share the one array: the scratch
 // is cleared at the start of every call (it keeps the previous call's
 // contents until then), and calls that overlap on the GPU -- on different
 // streams, or from different host threads -- race on it.
@@ -24,6 +27,10 @@
 namespace tg {
 
 constexpr size_t kNoAllocScratchBytes = (size_t)32 << 20;
+// The workspace of a deterministic backprojection is 256 header bytes plus 8
+// bytes per voxel, rounded up to 256 bytes; with a scratch size that is a
+// multiple of 256 the largest cube that fits is (scratch - 256) / 8 voxels.
+static_assert(kNoAllocScratchBytes % 256 == 0, "scratch size must be a multiple of 256 bytes");
 constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
@@ -49,5 +56,7 @@ cudaError_t noalloc_scratch(void **ptr) {
 }
 
 size_t noalloc_scratch_bytes() { return kNoAllocScratchBytes; }
+
+size_t noalloc_scratch_voxels() { return (kNoAllocScratchBytes - 256) / 8; }
 
 }  // namespace tg

@@ -92,6 +92,7 @@ cudaError_t launch_seg_axpby(float *y, const float *x, float alpha, float beta, 
                              cudaStream_t st);
 cudaError_t noalloc_scratch(void **ptr);
 size_t noalloc_scratch_bytes();
+size_t noalloc_scratch_voxels();
 cudaError_t launch_dot(const float *a, const float *b, long long n, double *partial, double *out, cudaStream_t s);
 
 }  // namespace tg

@@ -11,7 +11,9 @@ Tolerances (float32 GPU path against the float64 reference / oracle):
   sides).  A voxel below 1% of the maximum is made of a few short corner
   segments; a float32 segment length carries an absolute error of about one
   float32 ulp of the ray parameter (~5e-7 radii at the far side of a 3-radii
-  cube), which is not small relative to such a voxel;
+  cube), which is not small relative to such a voxel.  Sparse backprojections
+  (a few views) are checked per voxel only where a voxel holds at least a
+  quarter of one full-weight voxel chord (``cube_errors``);
 * adjoint: |<Px, y> - <x, P^T y>| / |<Px, y>| <= 1e-5.
 
 A ray is *degenerate* when a component of its direction is non-zero but
@@ -105,5 +107,53 @@ def image_errors(y, ref, exclude=None, sig=1e-3):
     return float(rel), float(norm)
 
 
+def cube_errors(c, ref, y_max, cdelt):
+    """(per-voxel max relative error, normwise error) of a backprojected cube.
+
+    The per-voxel error is taken over voxels whose reference value is at
+    least CUBE_SIG of the cube's maximum AND at least a quarter of one voxel
+    chord at full weight (cdelt * y_max / 4).  The second floor matters only
+    for sparse backprojections (a few views): a voxel below it holds only
+    short corner segments, whose float32 lengths carry an absolute error of
+    a few 1e-7 radii (the rounding of the crossing parameters), which no
+    float32 walk can make small relative to such a voxel.  With many views
+    (the workloads) the first floor is the larger one."""
+    c = np.asarray(c, np.float64)
+    ref = np.asarray(ref, np.float64)
+    scale = np.abs(ref).max()
+    if scale == 0:
+        return 0.0, float(np.abs(c).max())
+    d = np.abs(c - ref)
+    norm = d.max() / scale
+    big = np.abs(ref) >= max(CUBE_SIG * scale, 0.25 * cdelt * y_max)
+    rel = (d[big] / np.abs(ref[big])).max() if big.any() else 0.0
+    return float(rel), float(norm)
+
+
+def worst_element(y, ref, exclude=None, sig=1e-3):
+    """Where the per-element relative error of image_errors is largest:
+    (index, reference value / max |ref|, absolute error)."""
+    y = np.asarray(y, np.float64)
+    ref = np.asarray(ref, np.float64)
+    keep = np.ones(ref.shape, bool) if exclude is None else ~exclude
+    scale = np.abs(ref[keep]).max()
+    big = keep & (np.abs(ref) >= sig * scale)
+    r = np.where(big, np.abs(y - ref) / np.maximum(np.abs(ref), 1e-300), 0.0)
+    k = np.unravel_index(np.argmax(r), r.shape)
+    return [int(v) for v in k], float(ref[k] / scale), float(abs(y[k] - ref[k]))
+
+
 def rel_dot(a, b):
     return abs(a - b) / max(abs(a), abs(b), 1e-300)
+
+
+def record(name, **values):
+    """Append one measured-error record (JSON line) to the file named by the
+    TG_PARITY_REPORT environment variable, when it is set; the parity tests
+    call it so that a run can collect the errors it measured."""
+    path = os.environ.get("TG_PARITY_REPORT")
+    if not path:
+        return
+    import json
+    with open(path, "a") as f:
+        f.write(json.dumps(dict(test=name, **values)) + "\n")

@@ -506,3 +506,79 @@ def test_segment_counts_are_exact_integers():
     assert np.abs(counts - exact).max() <= 2
     assert np.mean(counts == exact) >= 0.99
     assert abs(counts.sum() - exact.sum()) <= 1e-3 * exact.sum() and counts.sum() > 0
+
+
+# --------------------------------------------------------------------------
+# per-ray and per-view diagnostics (tomograpy/siddon.py:221-243,341-350)
+
+def _diag_geometry():
+    ch, vh = _geometry(None, 4, 40, [0.3, 1.2, 2.6, 4.4], lat=[0.0, 0.2, -0.3, 0.1], rol=[0.0, 0.5, -1.0, 2.0],
+                       shape=(24, 20, 28), pshape=(3.0, 2.5, 3.5))
+    x = np.random.default_rng(17).random((24, 20, 28))
+    return ch, vh, x
+
+
+@pytest.mark.parametrize("obstacle", ["sun", None])
+def test_ray_projector_matches_oracle(obstacle):
+    """ray_projector traces one pixel's ray: that pixel gets the oracle's
+    value, every other pixel stays as it was; backprojecting one ray equals
+    the oracle's backprojection of a stack with only that pixel set; a mask
+    element equal to 1 skips the ray (the reference's test at
+    tomograpy/C_siddon.c.template:269-271)."""
+    ch, vh, x = _diag_geometry()
+    ref = InfoArray(shape=(40, 40, 4), header=_hdrs(vh))
+    oracle.projector(ref, InfoArray(data=x.astype(np.float32).astype(np.float64), header=dict(ch)),
+                     obstacle=obstacle)
+    degen = degenerate_rays(vh, 40, 40)
+    pixels = [(20, 20, 0), (3, 31, 1), (27, 8, 2), (39, 39, 3), (11, 19, 3)]
+    cube = InfoArray(data=x.astype(np.float32), header=dict(ch))
+    for (i, j, t) in pixels:
+        assert not degen[i, j, t]
+        data = InfoArray(shape=(40, 40, 4), header=_hdrs(vh), dtype=np.float32)
+        data[...] = -1.0
+        tg.ray_projector(data, cube, (i, j, t), obstacle=obstacle)
+        d = np.asarray(data, np.float64)
+        others = np.ones(d.shape, bool)
+        others[i, j, t] = False
+        assert np.all(d[others] == -1.0)
+        np.testing.assert_allclose(d[i, j, t] + 1.0, ref[i, j, t], rtol=IMG_TOL, atol=1e-6 * np.abs(ref).max())
+        # one ray backprojected
+        y = np.zeros((40, 40, 4), np.float32)
+        y[i, j, t] = 0.75
+        bc = InfoArray(shape=x.shape, header=dict(ch), dtype=np.float32)
+        tg.ray_projector(InfoArray(data=y, header=_hdrs(vh)), bc, (i, j, t), obstacle=obstacle, mode="bpj")
+        bref = InfoArray(shape=x.shape, header=dict(ch))
+        oracle.backprojector(InfoArray(data=y.astype(np.float64), header=_hdrs(vh)), bref, obstacle=obstacle)
+        rel, norm = image_errors(bc, bref, sig=CUBE_SIG)
+        assert norm <= CUBE_TOL, ((i, j, t), rel, norm)
+    # mask == 1 skips the ray
+    mask = np.zeros((40, 40, 4))
+    mask[20, 20, 0] = 1.0
+    data = InfoArray(shape=(40, 40, 4), header=_hdrs(vh), dtype=np.float32)
+    tg.ray_projector(data, cube, (20, 20, 0), mask=mask, obstacle=obstacle)
+    assert not np.asarray(data).any()
+
+
+def test_conic_image_backprojector_matches_oracle():
+    """Backprojecting view t alone equals the oracle's backprojection of the
+    stack with every other view zeroed, and the per-view cubes sum to the
+    full backprojection."""
+    ch, vh, x = _diag_geometry()
+    degen = degenerate_rays(vh, 40, 40)
+    y = np.random.default_rng(18).random((40, 40, 4)).astype(np.float32)
+    y[degen] = 0
+    total = np.zeros(x.shape)
+    for t in range(4):
+        cube = InfoArray(shape=x.shape, header=dict(ch), dtype=np.float32)
+        out = tg.conic_image_backprojector(InfoArray(data=y, header=_hdrs(vh)), cube, t, obstacle="sun")
+        assert out is cube
+        yt = np.zeros_like(y, dtype=np.float64)
+        yt[:, :, t] = y[:, :, t]
+        ref = InfoArray(shape=x.shape, header=dict(ch))
+        oracle.backprojector(InfoArray(data=yt, header=_hdrs(vh)), ref, obstacle="sun")
+        rel, norm = image_errors(cube, ref, sig=CUBE_SIG)
+        assert rel <= CUBE_TOL and norm <= CUBE_TOL, (t, rel, norm)
+        total += np.asarray(cube, np.float64)
+    full = InfoArray(shape=x.shape, header=dict(ch), dtype=np.float32)
+    tg.backprojector(InfoArray(data=y, header=_hdrs(vh)), full, obstacle="sun")
+    np.testing.assert_allclose(total, np.asarray(full, np.float64), rtol=1e-5, atol=1e-6 * np.abs(total).max())

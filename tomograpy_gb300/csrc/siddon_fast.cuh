@@ -46,11 +46,12 @@ namespace tg {
 
 // Compile-time tuning per direction (measured on GB300 at 256^3 x 360 x 512^2).
 // Both walk in drift batches (running-sum crossings, exact resynchronisation
-// per batch); the projection keeps a batch's gathers in registers (80
+// per batch); the projection issues each step's gather as the step is known
+// and keeps the batch's values in registers until the batch's sum (80
 // registers, 3 CTAs per SM), the backprojection issues each atomic at once
-// and so runs longer batches at 4 CTAs per SM (64 registers).
+// (64 registers, 4 CTAs per SM).
 #ifndef TG_PJ_BATCH
-#define TG_PJ_BATCH 20
+#define TG_PJ_BATCH 24
 #endif
 #ifndef TG_PJ_MIN_BLOCKS
 #define TG_PJ_MIN_BLOCKS 3
@@ -473,55 +474,146 @@ __device__ __forceinline__ float min3f(float a, float b, float c) {
   return r;
 }
 
+// Family advances are written as predicated PTX: per family one compare and
+// predicated updates that share its predicate (the three compares read the
+// crossings before any update, as in the reference's tie cases).
+//
+// Exact advance: every family whose next crossing equals tm takes its next
+// crossing fma(m + 1, p, d), and the voxel offset moves by its stride.
+template <typename IDX>
+__device__ __forceinline__ void advance_exact(Walk<IDX> &w, float tm) {
+  if constexpr (sizeof(IDX) == 4) {
+    asm("{\n\t.reg .pred p0, p1, p2;\n\t"
+        "setp.eq.f32 p0, %0, %7;\n\t"
+        "setp.eq.f32 p1, %1, %7;\n\t"
+        "setp.eq.f32 p2, %2, %7;\n\t"
+        "@p0 add.f32 %3, %3, 0f3F800000;\n\t"
+        "@p1 add.f32 %4, %4, 0f3F800000;\n\t"
+        "@p2 add.f32 %5, %5, 0f3F800000;\n\t"
+        "@p0 fma.rn.f32 %0, %3, %8, %11;\n\t"
+        "@p1 fma.rn.f32 %1, %4, %9, %12;\n\t"
+        "@p2 fma.rn.f32 %2, %5, %10, %13;\n\t"
+        "@p0 add.s32 %6, %6, %14;\n\t"
+        "@p1 add.s32 %6, %6, %15;\n\t"
+        "@p2 add.s32 %6, %6, %16;\n\t}"
+        : "+f"(w.t[0]), "+f"(w.t[1]), "+f"(w.t[2]), "+f"(w.m[0]), "+f"(w.m[1]), "+f"(w.m[2]), "+r"(w.off)
+        : "f"(tm), "f"(w.pa[0]), "f"(w.pa[1]), "f"(w.pa[2]), "f"(w.d[0]), "f"(w.d[1]), "f"(w.d[2]), "r"(w.st[0]),
+          "r"(w.st[1]), "r"(w.st[2]));
+  } else {
+    asm("{\n\t.reg .pred p0, p1, p2;\n\t"
+        "setp.eq.f32 p0, %0, %7;\n\t"
+        "setp.eq.f32 p1, %1, %7;\n\t"
+        "setp.eq.f32 p2, %2, %7;\n\t"
+        "@p0 add.f32 %3, %3, 0f3F800000;\n\t"
+        "@p1 add.f32 %4, %4, 0f3F800000;\n\t"
+        "@p2 add.f32 %5, %5, 0f3F800000;\n\t"
+        "@p0 fma.rn.f32 %0, %3, %8, %11;\n\t"
+        "@p1 fma.rn.f32 %1, %4, %9, %12;\n\t"
+        "@p2 fma.rn.f32 %2, %5, %10, %13;\n\t"
+        "@p0 add.s64 %6, %6, %14;\n\t"
+        "@p1 add.s64 %6, %6, %15;\n\t"
+        "@p2 add.s64 %6, %6, %16;\n\t}"
+        : "+f"(w.t[0]), "+f"(w.t[1]), "+f"(w.t[2]), "+f"(w.m[0]), "+f"(w.m[1]), "+f"(w.m[2]), "+l"(w.off)
+        : "f"(tm), "f"(w.pa[0]), "f"(w.pa[1]), "f"(w.pa[2]), "f"(w.d[0]), "f"(w.d[1]), "f"(w.d[2]), "l"(w.st[0]),
+          "l"(w.st[1]), "l"(w.st[2]));
+  }
+}
+
+// Running-sum advance (drift batches): an advancing family's local crossing
+// becomes tl + |p|.
+template <typename IDX>
+__device__ __forceinline__ void advance_drift(Walk<IDX> &w, float tl[3], float tm) {
+  if constexpr (sizeof(IDX) == 4) {
+    asm("{\n\t.reg .pred p0, p1, p2;\n\t"
+        "setp.eq.f32 p0, %0, %4;\n\t"
+        "setp.eq.f32 p1, %1, %4;\n\t"
+        "setp.eq.f32 p2, %2, %4;\n\t"
+        "@p0 add.f32 %0, %0, %5;\n\t"
+        "@p1 add.f32 %1, %1, %6;\n\t"
+        "@p2 add.f32 %2, %2, %7;\n\t"
+        "@p0 add.s32 %3, %3, %8;\n\t"
+        "@p1 add.s32 %3, %3, %9;\n\t"
+        "@p2 add.s32 %3, %3, %10;\n\t}"
+        : "+f"(tl[0]), "+f"(tl[1]), "+f"(tl[2]), "+r"(w.off)
+        : "f"(tm), "f"(w.pa[0]), "f"(w.pa[1]), "f"(w.pa[2]), "r"(w.st[0]), "r"(w.st[1]), "r"(w.st[2]));
+  } else {
+    asm("{\n\t.reg .pred p0, p1, p2;\n\t"
+        "setp.eq.f32 p0, %0, %4;\n\t"
+        "setp.eq.f32 p1, %1, %4;\n\t"
+        "setp.eq.f32 p2, %2, %4;\n\t"
+        "@p0 add.f32 %0, %0, %5;\n\t"
+        "@p1 add.f32 %1, %1, %6;\n\t"
+        "@p2 add.f32 %2, %2, %7;\n\t"
+        "@p0 add.s64 %3, %3, %8;\n\t"
+        "@p1 add.s64 %3, %3, %9;\n\t"
+        "@p2 add.s64 %3, %3, %10;\n\t}"
+        : "+f"(tl[0]), "+f"(tl[1]), "+f"(tl[2]), "+l"(w.off)
+        : "f"(tm), "f"(w.pa[0]), "f"(w.pa[1]), "f"(w.pa[2]), "l"(w.st[0]), "l"(w.st[1]), "l"(w.st[2]));
+  }
+}
+
 template <typename IDX>
 __device__ __forceinline__ float walk_step(Walk<IDX> &w, float &cur, IDX &seg_off) {
   const float tm = min3f(w.t[0], w.t[1], w.t[2]);
   const float L = tm - cur;
   seg_off = w.off;
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    if (w.t[k] == tm) {
-      w.m[k] += 1.f;
-      w.t[k] = fmaf(w.m[k], w.pa[k], w.d[k]);
-      w.off += w.st[k];
-    }
-  }
+  advance_exact(w, tm);
   cur = tm;
   return L;
 }
 
-// Step of a drift batch (projection): like walk_step, but an advanced family's
-// next crossing becomes t + |p| (one add instead of the count update and the
-// FMA) and the counts are not kept; resync() recovers them and recomputes
-// every crossing exactly after the batch.  Within a batch of kBatch steps
-// the running sums drift by at most kBatch / 2 ulp of |t|.
+// Step of a drift batch: like walk_step, but in a frame local to the batch
+// (tl = t - o with o the exact position where the batch starts), an advanced
+// family's next crossing becomes tl + |p| (one add instead of the count
+// update and the FMA) and the counts are not kept; resync() recovers them and
+// recomputes every crossing exactly after the batch.  The running sums stay
+// within the batch's extent of the origin, so their rounding (at most half an
+// ulp of that extent per add) does not grow with the distance from the chord
+// midpoint: measured at 256^3 x 512^2 (7 views), running sums in the
+// midpoint frame gave per-voxel backprojection errors up to 1.3e-4 and
+// per-pixel projection errors up to 7.2e-6, against 7.8e-5 / 3.0e-6 without
+// running sums.
 template <typename IDX>
-__device__ __forceinline__ float drift_step(Walk<IDX> &w, float &cur, IDX &seg_off) {
-  const float tm = min3f(w.t[0], w.t[1], w.t[2]);
-  const float L = tm - cur;
+__device__ __forceinline__ float drift_step(Walk<IDX> &w, float tl[3], float &cl, IDX &seg_off) {
+  const float tm = min3f(tl[0], tl[1], tl[2]);
+  const float L = tm - cl;
   seg_off = w.off;
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    if (w.t[k] == tm) {
-      w.t[k] += w.pa[k];
-      w.off += w.st[k];
-    }
-  }
-  cur = tm;
+  advance_drift(w, tl, tm);
+  cl = tm;
   return L;
 }
 
-// Exact counts and crossings after a drift batch: the drifted crossing is
-// within a few ulp of fma(m, p, d), so m = rint((t - d) / p).
+// Local frame of a drift batch starting at the exact position o.
 template <typename IDX>
-__device__ __forceinline__ void resync(Walk<IDX> &w) {
+__device__ __forceinline__ void to_local(const Walk<IDX> &w, float o, float tl[3]) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) tl[k] = w.t[k] - o;  // +inf stays +inf
+}
+
+// Exact counts and crossings after a drift batch: the drifted crossing
+// o + tl is within a few ulp of fma(m, p, d), so m = rint((o + tl - d) / p).
+template <typename IDX>
+__device__ __forceinline__ void resync(Walk<IDX> &w, const float tl[3], float o) {
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     if (w.pa[k] != __int_as_float(0x7f800000)) {
-      w.m[k] = rintf(__fdividef(w.t[k] - w.d[k], w.pa[k]));
+      w.m[k] = rintf(__fdividef((tl[k] + o) - w.d[k], w.pa[k]));
       w.t[k] = fmaf(w.m[k], w.pa[k], w.d[k]);
     }
   }
+}
+
+// The exact step that closes a drift batch: its crossing comes from the exact
+// (resynchronised) parameters, its start from the batch's local frame, so the
+// segment length is (tm - o) - cl; `cur` leaves it exact.
+template <typename IDX>
+__device__ __forceinline__ float close_step(Walk<IDX> &w, float o, float cl, float &cur, IDX &seg_off) {
+  const float tm = min3f(w.t[0], w.t[1], w.t[2]);
+  const float L = (tm - o) - cl;
+  seg_off = w.off;
+  advance_exact(w, tm);
+  cur = tm;
+  return L;
 }
 
 // Internal mode: count the steps each ray takes (written to xout as float;
@@ -611,16 +703,17 @@ __device__ __forceinline__ void trace_fast(const Geometry &G, const tg_image_hea
   // the batch is exactly kBatch iterations of the single-step loop below, with
   // no per-step test, and its kBatch cube gathers are issued together.
   //
-  // Projection batches drift (drift_step): their first kBatch - 1 crossings
-  // are running sums.  Every sum that can be taken lies in [-h, h] (h = half
-  // chord), so each add is off by at most 2^-24 h and a drifted crossing by at
-  // most (kBatch - 1) 2^-24 h; the bound gets a margin of (kBatch + 1) 2^-23 h,
-  // more than twice that, so a drifted step still advances only families
+  // Drift batches (drift_step): their first kBatch - 1 crossings are running
+  // sums in the batch's local frame tl = t - o.  Every crossing that matters
+  // lies in [-h, h] (h = half chord), so |tl| <= 2h: the conversion to the
+  // local frame and each add are off by at most 2^-24 (2h), and a drifted
+  // crossing by at most kBatch 2^-23 h; the bound gets a margin of
+  // (kBatch + 3) 2^-23 h, so a drifted step still advances only families
   // whose exact crossing is below the stop.  The counts are then recovered
   // (resync) and the batch's last step is an exact one.
   constexpr int kBatch = batch_steps(MODE);
   constexpr bool kDrift = drift_batches(MODE);
-  const float margin = kDrift ? (float)(kBatch + 1) * 1.1920929e-7f * (-w.t0) : 0.f;
+  const float margin = kDrift ? (float)(kBatch + 3) * 1.1920929e-7f * (-w.t0) : 0.f;
   while (guard >= kBatch) {
     const float bnd = min3f(fmaf(w.m[0] + (float)(kBatch - 2), w.pa[0], w.d[0]),
                             fmaf(w.m[1] + (float)(kBatch - 2), w.pa[1], w.d[1]),
@@ -631,15 +724,18 @@ __device__ __forceinline__ void trace_fast(const Geometry &G, const tg_image_hea
       // backprojection: each segment's atomic is issued as soon as the step
       // is known (fire-and-forget, so nothing is kept per step)
       if (kDrift) {
+        const float org = cur;
+        float tl[3], cl = 0.f;
+        to_local(w, org, tl);
 #pragma unroll
         for (int s = 0; s < kBatch - 1; ++s) {
           IDX o;
-          const float L = drift_step(w, cur, o);
+          const float L = drift_step(w, tl, cl, o);
           accumulate<MODE, DET, IDX>(L, o, cin, cout, aout, yv, yq, qs, acc);
         }
-        resync(w);
+        resync(w, tl, org);
         IDX o;
-        const float L = walk_step(w, cur, o);
+        const float L = close_step(w, org, cl, cur, o);
         accumulate<MODE, DET, IDX>(L, o, cin, cout, aout, yv, yq, qs, acc);
       } else {
 #pragma unroll
@@ -652,25 +748,32 @@ __device__ __forceinline__ void trace_fast(const Geometry &G, const tg_image_hea
       continue;
     }
     float L[kBatch];
-    IDX o[kBatch];
+    float v[kBatch];
     if (kDrift) {
-      // the batch's last step is exact, so `cur` leaves the batch exact and
-      // the stop test after it compares exact values (a drifted crossing just
-      // below an exact exit would let the next step read outside the cube)
+      const float org = cur;
+      float tl[3], cl = 0.f;
+      to_local(w, org, tl);
 #pragma unroll
-      for (int s = 0; s < kBatch - 1; ++s) L[s] = drift_step(w, cur, o[s]);
-      resync(w);
-      L[kBatch - 1] = walk_step(w, cur, o[kBatch - 1]);
+      for (int s = 0; s < kBatch - 1; ++s) {
+        IDX os;
+        L[s] = drift_step(w, tl, cl, os);
+        v[s] = CNT ? 1.f : __ldg(cin + os);
+      }
+      resync(w, tl, org);
+      IDX os;
+      L[kBatch - 1] = close_step(w, org, cl, cur, os);
+      v[kBatch - 1] = CNT ? 1.f : __ldg(cin + os);
     } else {
 #pragma unroll
-      for (int s = 0; s < kBatch; ++s) L[s] = walk_step(w, cur, o[s]);
+      for (int s = 0; s < kBatch; ++s) {
+        IDX os;
+        L[s] = walk_step(w, cur, os);
+        v[s] = CNT ? 1.f : __ldg(cin + os);
+      }
     }
     if (CNT) {
       acc += (float)kBatch;
     } else {
-      float v[kBatch];
-#pragma unroll
-      for (int s = 0; s < kBatch; ++s) v[s] = __ldg(cin + o[s]);
       float part = L[0] * v[0];
 #pragma unroll
       for (int s = 1; s < kBatch; ++s) part = fmaf(L[s], v[s], part);

@@ -5,7 +5,7 @@ A drop-in for the hot path of TomograPy (``tomograpy.projector``,
 the ``lo_wrapper`` linear operators): the same Python API over hand-written
 CUDA kernels reached through a C ABI (``include/tomograpy_gb300.h``).
 """
-from . import headers, simu, synthetic
+from . import headers, simu, solar, synthetic
 from .headers import (INF, apply_rotation, array_to_dict, centered_cubic_map, centered_cubic_map_header,
                       centered_image, centered_image_header, centered_stack, dataarray_from_header,
                       dict_to_array, fov, full_intersection_parameters, full_rotation_matrix,

@@ -20,7 +20,9 @@ Steps (mirroring what ``tomograpy/parse_templates.py:11-34`` and
 4. write only the resulting ``.so`` files into ``oracle/_ref/``.
 
 The expanded sources stay in the temporary directory; ``oracle/_ref/`` is
-git-ignored.  Run: ``python oracle/build_ref.py [--reference PATH]``.
+git-ignored.  Run: ``python oracle/build_ref.py [--reference PATH]`` (default:
+``$TOMOGRAPY_REFERENCE``, else a checkout named ``reference`` beside the
+repository).
 """
 import argparse
 import os
@@ -32,7 +34,10 @@ from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-DEFAULT_REFERENCE = "/root/reference"
+# The reference checkout: $TOMOGRAPY_REFERENCE, else a directory named
+# "reference" beside this repository's root.
+DEFAULT_REFERENCE = os.environ.get("TOMOGRAPY_REFERENCE") or \
+    os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 
 CTYPES = ("float", "double")
 OBSTACLES = ("none", "sun")

@@ -177,7 +177,9 @@ class Server:
         self._limbo = []         # (steps launched at retirement, slot)
         self._steps = []         # queued steps: (event, pinned r.r, slots, step number)
         self._results = []       # (request, pinned cube, event)
-        self.host_s = {"admit": 0.0, "rebuild": 0.0, "step": 0.0, "retire": 0.0, "collect": 0.0}
+        # host seconds per activity; "wait" is time blocked on the GPU (the
+        # events of queued steps), "retire" the retirement work around it
+        self.host_s = {"admit": 0.0, "rebuild": 0.0, "step": 0.0, "retire": 0.0, "wait": 0.0, "collect": 0.0}
         self.rebuilds = 0
 
     # admission -------------------------------------------------------------
@@ -314,7 +316,9 @@ class Server:
         than `keep_queued` steps are queued."""
         while self._steps and (len(self._steps) > keep_queued or self._steps[0][0].query()):
             ev, rel, jobs, step_no = self._steps.pop(0)
+            t0 = time.perf_counter()
             ev.synchronize()
+            self.host_s["wait"] += time.perf_counter() - t0
             bb = self.bb_host.numpy()[[job.slot for job in jobs]]
             vals = np.sqrt(rel.numpy() / bb)
             for job, r in zip(jobs, vals):
@@ -416,8 +420,9 @@ class Server:
                 continue
             self.step()
             t0 = time.perf_counter()
+            w0 = self.host_s["wait"]
             self.retire()
-            self.host_s["retire"] += time.perf_counter() - t0
+            self.host_s["retire"] += (time.perf_counter() - t0) - (self.host_s["wait"] - w0)
         self._read_residuals(keep_queued=0)
         self._collect(wait=True)
         torch.cuda.synchronize()

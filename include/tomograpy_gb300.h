@@ -221,6 +221,9 @@ typedef struct {
   int32_t four_d;
   int32_t idx64;
   int64_t tiles;                 /* CTAs of one packed launch */
+  int64_t det_workspace_bytes;   /* workspace of tg_packed_backprojector_deterministic */
+  int32_t det_idx64;             /* a job's accumulator needs 64-bit offsets */
+  int32_t reserved;
 } tg_packed_info;
 
 size_t tg_packed_plan_bytes(int32_t n_jobs);
@@ -233,6 +236,15 @@ tg_status tg_packed_plan_host(const tg_job *jobs, int32_t n_jobs, int32_t rows_p
                               void *host_plan, size_t plan_bytes, tg_packed_info *info);
 tg_status tg_packed_projector(const void *plan, const tg_packed_info *info, int32_t mode, int32_t obstacle,
                               void *stream);
+/* Deterministic packed backprojection (TG_BPJ, or TG_BPJT for a 4-D plan):
+ * every job's cube gets, added in place, exactly the result of
+ * tg_conic_full_backprojector_deterministic on that job alone (per-job
+ * fixed-point scale, order-independent integer sums), so a job's result does
+ * not depend on the other jobs of the plan.  Workspace:
+ * info->det_workspace_bytes bytes, 256-byte aligned, cleared by the call.
+ * No counterpart in the reference. */
+tg_status tg_packed_backprojector_deterministic(const void *plan, const tg_packed_info *info, int32_t obstacle,
+                                               void *workspace, size_t workspace_bytes, void *stream);
 
 /* Segmented float64-accumulated inner products over float32 buffers:
  * out[s] = sum_{i in [seg[2s], seg[2s+1])} a[i] b[i] for s < n_seg (seg:

@@ -38,7 +38,7 @@ def test_symbol_exported(lib, name):
 
 
 def test_abi_version(lib):
-    assert lib.tg_abi_version() == 1
+    assert lib.tg_abi_version() == 2
 
 
 def test_workspace_size(lib):

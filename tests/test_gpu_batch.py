@@ -118,3 +118,57 @@ def test_packed_time_dependent_jobs_match_single_job():
         ref = ops[k].backproject(pack.data_view(pack.data, k).contiguous())
         rel, norm = image_errors(pack.cube_view(z, k).cpu().numpy(), ref.cpu().numpy(), sig=CUBE_SIG)
         assert rel <= CUBE_TOL and norm <= CUBE_TOL, (k, rel, norm)
+
+
+# --------------------------------------------------------------------------
+# deterministic (fixed-point) backprojection: bitwise isolation
+
+def test_packed_deterministic_backprojection_equals_single_job_bitwise():
+    """tg_packed_backprojector_deterministic gives every job exactly the
+    single-job deterministic backprojection (3-D and time-dependent packs)."""
+    jobs, pack = _pack(2)
+    rng = np.random.default_rng(4)
+    for k, j in enumerate(jobs):
+        pack.data_view(pack.data, k).copy_(torch.from_numpy(rng.random(j.data_shape).astype(np.float32)))
+    z = pack.backproject(pack.new_cube(), deterministic=True)
+    for k, j in enumerate(jobs):
+        op = lo_wrapper.siddon_lo(j.view_headers, j.cube_header, obstacle="sun", dtype=np.float32, deterministic=True)
+        ref = op.backproject(pack.data_view(pack.data, k).contiguous())
+        assert torch.equal(pack.cube_view(z, k), ref), k
+    # time-dependent jobs: frame-major 4-D accumulators
+    specs = [(dict(n=16, T=6, N=32, d=200.0, lon_range=(0.1, 3.0), n_frames=3), 2),
+             (dict(n=24, T=8, N=48, d=180.0, lon_range=(0.4, 5.0), n_frames=2), 4)]
+    jobs4, ops4 = [], []
+    for sp, ng in specs:
+        ch, vh = synthetic.make_geometry(sp)
+        jobs4.append(batch.Job(ch, vh, frames=np.arange(sp["T"]) // ng))
+        ops4.append(lo_wrapper.siddon4d_lo(vh, ch, ng=ng, obstacle="sun", dtype=np.float32, deterministic=True))
+    pack4 = batch.PackedJobs(jobs4, obstacle="sun", rows_per_warp=1)
+    for k, j in enumerate(jobs4):
+        pack4.data_view(pack4.data, k).copy_(torch.from_numpy(rng.random(j.data_shape).astype(np.float32)))
+    z4 = pack4.backproject(pack4.new_cube(), deterministic=True)
+    for k in range(len(jobs4)):
+        ref = ops4[k].backproject(pack4.data_view(pack4.data, k).contiguous())
+        assert torch.equal(pack4.cube_view(z4, k), ref), k
+
+
+def test_deterministic_cg_is_bitwise_isolated():
+    """With fixed-point backprojections, a job's 20th CG iterate is bitwise
+    the same in a batch of four, alone in a batch and in the plain per-job
+    loop (the float-atomic path differs by up to ~1e-2 at 20 iterations)."""
+    jobs, pack = _pack()
+    x_true = pack.new_cube()
+    for k, j in enumerate(jobs):
+        pack.cube_view(x_true, k).copy_(torch.from_numpy(j.phantom))
+    pack.project(x_true)
+    b = pack.backproject(pack.new_cube(), deterministic=True)
+    x, _ = batch.batched_cg(pack, b, lam=1e-2, iters=20, graph=True, deterministic=True)
+    seq = batch.sequential_cg(jobs, [pack.cube_view(b, k).clone() for k in range(len(jobs))], iters=20,
+                              deterministic=True)
+    for k in range(len(jobs)):
+        assert torch.equal(pack.cube_view(x, k), seq[k]), k
+    alone = batch.PackedJobs([jobs[3]], obstacle="sun", rows_per_warp=pack.rows_per_warp)
+    ba = alone.new_cube()
+    ba.copy_(pack.cube_view(b, 3).reshape(-1))
+    xa, _ = batch.batched_cg(alone, ba, lam=1e-2, iters=20, graph=False, deterministic=True)
+    assert torch.equal(xa, pack.cube_view(x, 3).reshape(-1))

@@ -85,3 +85,25 @@ def test_request_larger_than_budget_is_refused():
     srv = serve.Server(budget_bytes=4096)
     with pytest.raises(RuntimeError, match="does not fit"):
         srv.run(reqs)
+
+
+def test_deterministic_serving_is_bitwise_isolated():
+    """With fixed-point backprojections a served request's 20-iteration result
+    is bitwise the same in the mix, served alone and in the FIFO plain loop."""
+    budget = 256 << 20
+    reqs = serve.poisson_requests(SPECS, rate=1.0, seed=0, max_iters=20, tol=0.0)
+    for r, t in zip(reqs, [0.0, 0.0, 0.001, 0.002, 0.003]):
+        r.arrival = t
+    srv = serve.Server(budget_bytes=budget, deterministic=True)
+    srv.run(reqs)
+    assert srv.max_inflight >= 2
+    plain = serve.poisson_requests(SPECS, rate=1.0, seed=0, max_iters=20, tol=0.0)
+    for r in plain:
+        r.arrival = 0.0
+    serve.fifo_plain(plain, deterministic=True)
+    for r, p in zip(reqs, plain):
+        assert r.iters == 20 and p.iters == 20
+        a = serve.Request(r.id, r.job, r.data, 0.0, 20, 0.0)
+        serve.Server(budget_bytes=budget, deterministic=True).run([a])
+        assert torch.equal(r.result, a.result), r.id
+        assert torch.equal(r.result, p.result), r.id

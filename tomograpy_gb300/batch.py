@@ -43,7 +43,8 @@ class TgJob(ctypes.Structure):
 
 class TgPackedInfo(ctypes.Structure):
     _fields_ = [("n_jobs", ctypes.c_int32), ("rows_per_warp", ctypes.c_int32), ("four_d", ctypes.c_int32),
-                ("idx64", ctypes.c_int32), ("tiles", ctypes.c_int64)]
+                ("idx64", ctypes.c_int32), ("tiles", ctypes.c_int64), ("det_workspace_bytes", ctypes.c_int64),
+                ("det_idx64", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 def _bind(L):
@@ -58,6 +59,8 @@ def _bind(L):
     L.tg_packed_plan_host.restype = ctypes.c_int
     L.tg_packed_projector.argtypes = [P, P, I32, I32, P]
     L.tg_packed_projector.restype = ctypes.c_int
+    L.tg_packed_backprojector_deterministic.argtypes = [P, P, I32, P, SZ, P]
+    L.tg_packed_backprojector_deterministic.restype = ctypes.c_int
     L.tg_segmented_workspace_bytes.argtypes = [I32]
     L.tg_segmented_workspace_bytes.restype = SZ
     L.tg_segmented_dot_f32.argtypes = [P, P, P, I32, P, P, SZ, P]
@@ -132,6 +135,7 @@ class PackedJobs:
         self.mhs = [S.pack_map_header(j.cube_header) for j in self.jobs]
         self.data = torch.zeros(int(self.data_off[-1]), dtype=torch.float32, device=dev)
         self._plans = {}
+        self._det_ws = None
         self.rows_per_warp = rows_per_warp or self.autotune()
 
     # views of the flat buffers -------------------------------------------------
@@ -194,10 +198,21 @@ class PackedJobs:
                                               _lib.OBSTACLES[self.obstacle], _stream()))
         return self.data
 
-    def backproject(self, cube_flat, rows_per_warp=None):
-        """cube_flat = P^T self.data (all jobs, one launch; cube zeroed first)."""
+    def backproject(self, cube_flat, rows_per_warp=None, deterministic=False):
+        """cube_flat = P^T self.data (all jobs, one launch; cube zeroed first).
+        ``deterministic``: every job's cube is bitwise the single-job
+        deterministic backprojection of that job alone
+        (``tg_packed_backprojector_deterministic``), whatever the other jobs."""
         buf, info, _ = self.plan(cube_flat, rows_per_warp)
         cube_flat.zero_()
+        if deterministic:
+            need = int(info.det_workspace_bytes)
+            if self._det_ws is None or self._det_ws.numel() < need:
+                self._det_ws = torch.empty(need, dtype=torch.uint8, device=self.device)
+            _lib.check(self.L.tg_packed_backprojector_deterministic(
+                _ptr(buf), ctypes.byref(info), _lib.OBSTACLES[self.obstacle], _ptr(self._det_ws),
+                self._det_ws.numel(), _stream()))
+            return cube_flat
         _lib.check(self.L.tg_packed_projector(_ptr(buf), ctypes.byref(info),
                                               _lib.TG_BPJT if self.four_d else _lib.TG_BPJ,
                                               _lib.OBSTACLES[self.obstacle], _stream()))
@@ -231,9 +246,12 @@ class PackedJobs:
         return best
 
 
-def batched_cg(pack, b, lam=1e-2, iters=20, graph=True):
+def batched_cg(pack, b, lam=1e-2, iters=20, graph=True, deterministic=False):
     """CG on every job's (P^T P + lam I) x = b at once (b, x: flat cube buffers).
-    Returns (x, residual history (iters + 1, n_jobs) of ||r|| / ||b||)."""
+    Returns (x, residual history (iters + 1, n_jobs) of ||r|| / ||b||).
+    With ``deterministic`` the backprojections are the fixed-point ones, so
+    every job's iterates are bitwise those of the same job solved alone (here
+    or with :func:`sequential_cg` and a deterministic operator)."""
     from .cg import SegmentOps
     dev = pack.device
     n = pack.n
@@ -256,9 +274,9 @@ def batched_cg(pack, b, lam=1e-2, iters=20, graph=True):
 
     def step():
         pack.project(p)
-        pack.backproject(Ap)
+        pack.backproject(Ap, deterministic=deterministic)
         if lam:
-            Ap.add_(p, alpha=lam)
+            ops.axpby(Ap, p, lam, 1.0)          # Ap = lam p + Ap, one fmaf per element
         ops.dot(p, Ap, pAp)
         ops.update_x(x, r, p, Ap, rr, pAp)
         ops.dot(r, r, rr_new)
@@ -286,14 +304,14 @@ def batched_cg(pack, b, lam=1e-2, iters=20, graph=True):
     return x, hist
 
 
-def sequential_cg(jobs, rhs, lam=1e-2, iters=20, device=None):
+def sequential_cg(jobs, rhs, lam=1e-2, iters=20, device=None, deterministic=False):
     """The plain per-job loop: one job after another, each with its own
     operator and CG (tomograpy_gb300.cg), single-job kernel launches."""
     from . import cg, lo_wrapper
     out = []
     for j, b in zip(jobs, rhs):
         op = lo_wrapper.siddon_lo(j.view_headers, j.cube_header, obstacle=j.obstacle, dtype=np.float32,
-                                  device=device)
+                                  device=device, deterministic=deterministic)
         res = cg.cg(cg.NormalOperator(op, lam=lam), b, maxiter=iters)
         out.append(res.x)
     return out

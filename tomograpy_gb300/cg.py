@@ -63,6 +63,7 @@ class NormalOperator:
 
     def __init__(self, P, lam=0.0, hypers=(), temporal=0.0):
         self.P = P
+        self._ops, self._ops_n = None, 0
         self.lam = float(lam)
         self.hypers = tuple(float(h) for h in hypers)
         self.temporal = float(temporal)
@@ -71,7 +72,14 @@ class NormalOperator:
         y = self.P.project(x)
         out = self.P.backproject(y)
         if self.lam:
-            out.add_(x, alpha=self.lam)
+            if out.stride() == x.stride() and out.dtype == torch.float32 and dense(x):
+                # out = lam x + out as one fmaf per element, the arithmetic of
+                # the batched and served solvers (tg_segmented_axpby)
+                if self._ops is None or self._ops_n != x.numel():
+                    self._ops, self._ops_n = SegmentOps([0, x.numel()], x.device), x.numel()
+                self._ops.axpby(out, x, self.lam, 1.0)
+            else:
+                out.add_(x, alpha=self.lam)
         for axis, h in enumerate(self.hypers):
             if h:
                 out.add_(diff_normal(x, axis), alpha=h)

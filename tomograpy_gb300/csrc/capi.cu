@@ -357,13 +357,21 @@ static tg_status build_packed_plan(const tg_job *jobs, int32_t n_jobs, int32_t r
   std::stable_sort(order.begin(), order.end(), [](const Item &a, const Item &b) { return a.work > b.work; });
   const size_t rec0 = tg::packed_records_offset(n_jobs);
   long long tiles = 0;
+  size_t ws = 0;             // deterministic workspace: one 256-byte aligned part per job
+  bool det_idx64 = false;
   for (int k = 0; k < n_jobs; ++k) {
     const int j = order[k].idx;
     const tg_job &J = jobs[j];
     const int gx = (int)((J.n2 + 31) / 32), gy = (int)((J.n1 + rows - 1) / rows);
+    const int64_t shape4[4] = {J.map_shape[0], J.map_shape[1], J.map_shape[2], four_d ? J.map_shape[3] : 1};
+    const size_t part = tg_deterministic_workspace_bytes(shape4);
+    if (part == SIZE_MAX || ws > SIZE_MAX - part) return fail(TG_EINVAL, "job %d: cube too large", j);
+    det_idx64 = det_idx64 || (double)J.map_shape[0] * J.map_shape[1] * J.map_shape[2] >= 2147483647.0;
     std::memcpy(host + (size_t)k * sizeof(long long), &tiles, sizeof(long long));
-    tg::packed_fill(host + rec0 + (size_t)k * tg::packed_job_bytes(), geoms[j], J.data, J.map, tiles, gx, gy);
+    tg::packed_fill(host + rec0 + (size_t)k * tg::packed_job_bytes(), geoms[j], J.data, J.map, tiles, gx, gy,
+                    (long long)ws);
     tiles += (long long)gx * gy * J.n_views;
+    ws += part;
   }
   if (tiles > 2147483647LL) return fail(TG_EUNSUPPORTED, "packed launch of %lld CTAs is too large", tiles);
   info->n_jobs = n_jobs;
@@ -371,6 +379,9 @@ static tg_status build_packed_plan(const tg_job *jobs, int32_t n_jobs, int32_t r
   info->four_d = four_d != 0;
   info->idx64 = idx64 ? 1 : 0;
   info->tiles = tiles;
+  info->det_workspace_bytes = (int64_t)ws;
+  info->det_idx64 = det_idx64 ? 1 : 0;
+  info->reserved = 0;
   return TG_OK;
 }
 
@@ -386,6 +397,23 @@ tg_status tg_packed_projector(const void *plan, const tg_packed_info *info, int3
   return launch_status(tg::launch_packed(plan, info->n_jobs, info->tiles, info->rows_per_warp, info->idx64 != 0,
                                          mode, obstacle, (cudaStream_t)stream),
                        "packed projector launch");
+}
+
+tg_status tg_packed_backprojector_deterministic(const void *plan, const tg_packed_info *info, int32_t obstacle,
+                                               void *workspace, size_t workspace_bytes, void *stream) {
+  if (!plan || !info) return fail(TG_EINVAL, "NULL plan");
+  if (obstacle != TG_OBSTACLE_NONE && obstacle != TG_OBSTACLE_SUN)
+    return fail(TG_EINVAL, "obstacle must be none or sun");
+  if (info->n_jobs <= 0 || info->n_jobs > 65535) return fail(TG_EINVAL, "plan has %d jobs (1 to 65535)", info->n_jobs);
+  if (info->tiles <= 0) return TG_OK;
+  if (!workspace || ((uintptr_t)workspace & 255u)) return fail(TG_EINVAL, "workspace must be 256-byte aligned");
+  if (info->det_workspace_bytes <= 0 || workspace_bytes < (size_t)info->det_workspace_bytes)
+    return fail(TG_ENOMEM, "workspace has %zu bytes, the plan needs %lld", workspace_bytes,
+                (long long)info->det_workspace_bytes);
+  return launch_status(tg::launch_packed_det(plan, info->n_jobs, info->tiles, info->rows_per_warp,
+                                             info->idx64 != 0 || info->det_idx64 != 0, info->four_d != 0, obstacle,
+                                             workspace, (size_t)info->det_workspace_bytes, (cudaStream_t)stream),
+                       "deterministic packed backprojection launch");
 }
 
 size_t tg_segmented_workspace_bytes(int32_t n_seg) { return n_seg > 0 ? tg::seg_workspace_bytes(n_seg) : 0; }
@@ -460,6 +488,6 @@ tg_status tg_dot_f32(const float *a, const float *b, int64_t n, double *out, voi
 
 const char *tg_last_error(void) { return g_err; }
 
-int32_t tg_abi_version(void) { return 1; }
+int32_t tg_abi_version(void) { return 2; }
 
 }  // extern "C"

@@ -12,59 +12,22 @@
 //
 // Workspace layout (256-byte aligned): [DetScale | pad to 256 B |
 // int64 accumulator, dense C order (F, n0, n1, n2)].
-#include "siddon_fast.cuh"
+#include "det_common.cuh"
 
 namespace tg {
 
 __global__ void det_prepass_kernel(const Geometry G, const float *__restrict__ data, int n_views,
                                    DetScale *__restrict__ dsc) {
-  const long long total = (long long)G.n1 * G.n2 * n_views;
-  float m = 0.f;
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < total;
-       p += (long long)gridDim.x * blockDim.x) {
-    const int j = (int)(p % G.n2);
-    const long long r = p / G.n2;
-    const int i = (int)(r % G.n1);
-    const int t = G.view0 + (int)(r / G.n1);
-    if (masked(G, i, j, t)) continue;
-    const float v = fabsf(data[(long long)i * G.ds[0] + (long long)j * G.ds[1] + (long long)t * G.ds[2]]);
-    m = fmaxf(m, v);
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(&dsc->ymax_bits, __float_as_uint(m));
+  det_prepass_range(G, data, n_views, dsc, blockIdx.x * (long long)blockDim.x + threadIdx.x,
+                    (long long)gridDim.x * blockDim.x);
 }
 
-__global__ void det_scale_kernel(DetScale *dsc, double rays, double lmax) {
-  const float ymax = __uint_as_float(dsc->ymax_bits);
-  int e = 0;
-  if (ymax > 0.f && isfinite(ymax)) frexpf(ymax, &e);
-  const double bound = fmax(rays * lmax, 1e-30);
-  int s = (int)floor(61.0 - log2(bound));
-  s = max(-100, min(100, s));
-  dsc->yscale = ldexpf(1.f, -e);
-  dsc->qscale = ldexpf(1.f, s);
-  dsc->out_scale = ldexp(1.0, e - s);
-}
+__global__ void det_scale_kernel(DetScale *dsc, double rays, double lmax) { det_scale(dsc, rays, lmax); }
 
 __global__ void det_finalize_kernel(const Geometry G, const long long *__restrict__ acc,
                                     const DetScale *__restrict__ dsc, float *__restrict__ map) {
-  const long long nvox = (long long)G.n[0] * G.n[1] * G.n[2];
-  const long long total = nvox * G.nframes;
-  const double sc = dsc->out_scale;
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < total;
-       p += (long long)gridDim.x * blockDim.x) {
-    const long long q = acc[p];
-    if (q == 0) continue;
-    const long long f = p / nvox;
-    long long r = p - f * nvox;
-    const int z = (int)(r % G.n[2]);
-    r /= G.n[2];
-    const int y = (int)(r % G.n[1]);
-    const int x = (int)(r / G.n[1]);
-    const long long o = (long long)x * G.ms[0] + (long long)y * G.ms[1] + (long long)z * G.ms[2] + f * G.ms[3];
-    map[o] += (float)((double)q * sc);
-  }
+  det_finalize_range(G, acc, dsc, map, blockIdx.x * (long long)blockDim.x + threadIdx.x,
+                     (long long)gridDim.x * blockDim.x);
 }
 
 cudaError_t launch_deterministic_bpj(const Geometry &G, int mode, int obstacle, bool idx64, const float *data,
@@ -82,16 +45,10 @@ cudaError_t launch_deterministic_bpj(const Geometry &G, int mode, int obstacle, 
   if (pblocks > 152 * 16) pblocks = 152 * 16;
   if (pblocks < 1) pblocks = 1;
   det_prepass_kernel<<<pblocks, 256, 0, s>>>(G, data, gz, dsc);
-  double lmax = 0.0;
-  for (int k = 0; k < 3; ++k) lmax += G.mh.cdelt[k] * G.mh.cdelt[k];
-  lmax = sqrt(lmax);
-  det_scale_kernel<<<1, 1, 0, s>>>(dsc, (double)total, lmax);
+  det_scale_kernel<<<1, 1, 0, s>>>(dsc, (double)total, det_lmax(G));
   // walk with accumulator strides (dense C order, frame-major)
   Geometry A = G;
-  A.ms[2] = 1;
-  A.ms[1] = G.n[2];
-  A.ms[0] = (long long)G.n[1] * G.n[2];
-  A.ms[3] = nvox;
+  det_acc_strides(G, A.ms);
   const dim3 grid(gx, gy, gz);
   unsigned long long *a64 = (unsigned long long *)acc;
   const bool t4 = (mode == TG_BPJT);

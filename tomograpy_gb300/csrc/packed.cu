@@ -8,7 +8,7 @@
 // finds its job by binary search on the compact tile array, copies the job's
 // record into shared memory and runs the same tile body as the single-job
 // kernel.
-#include "siddon_fast.cuh"
+#include "det_common.cuh"
 
 namespace tg {
 
@@ -16,13 +16,20 @@ struct PackedJob {
   Geometry G;
   float *data;
   float *cube;
-  long long tile0;  // first CTA tile of this job
-  int gx, gy;       // column / row tiles per view
+  long long tile0;      // first CTA tile of this job
+  int gx, gy;           // column / row tiles per view
+  // deterministic backprojection: the job's part of the workspace (byte
+  // offset: DetScale, then its int64 accumulator at +256), the accumulator's
+  // dense strides, and the ray count and voxel diagonal behind its scale
+  long long ws_off;
+  long long acc_ms[4];
+  double rays, lmax;
 };
 
-template <int MODE, bool SUN, typename IDX, int RPW>
+template <int MODE, bool SUN, typename IDX, int RPW, bool DET>
 __global__ void __launch_bounds__(kThreads, min_blocks(MODE))
-    packed_kernel(const long long *__restrict__ tile0, const PackedJob *__restrict__ jobs, int n_jobs) {
+    packed_kernel(const long long *__restrict__ tile0, const PackedJob *__restrict__ jobs, int n_jobs,
+                  unsigned char *__restrict__ ws) {
   static_assert(sizeof(PackedJob) % 4 == 0, "job record copied as 32-bit words");
   __shared__ int s_job;
   __shared__ __align__(16) int s_rec[sizeof(PackedJob) / 4];
@@ -40,30 +47,60 @@ __global__ void __launch_bounds__(kThreads, min_blocks(MODE))
   const int *src = reinterpret_cast<const int *>(jobs + s_job);
   for (int k = threadIdx.x; k < (int)(sizeof(PackedJob) / 4); k += blockDim.x) s_rec[k] = __ldg(src + k);
   __syncthreads();
-  const PackedJob &J = *reinterpret_cast<const PackedJob *>(s_rec);
+  PackedJob &J = *reinterpret_cast<PackedJob *>(s_rec);
+  if (DET) {  // the walk indexes the job's dense accumulator instead of its cube
+    if (threadIdx.x < 4) J.G.ms[threadIdx.x] = J.acc_ms[threadIdx.x];
+    __syncthreads();
+  }
   long long local = (long long)blockIdx.x - J.tile0;
   const int bx = (int)(local % J.gx);
   local /= J.gx;
   const int by = (int)(local % J.gy);
   const int t = (int)(local / J.gy);
   constexpr bool PJ = (MODE == TG_PJ || MODE == TG_PJT);
-  tile_body<MODE, SUN, IDX, false, RPW>(J.G, t, bx * 32, by * (RPW * kRows), PJ ? J.cube : J.data,
-                                        PJ ? J.data : J.cube, nullptr, nullptr);
+  unsigned long long *acc = DET ? reinterpret_cast<unsigned long long *>(ws + J.ws_off + 256) : nullptr;
+  const DetScale *dsc = DET ? reinterpret_cast<const DetScale *>(ws + J.ws_off) : nullptr;
+  tile_body<MODE, SUN, IDX, DET, RPW>(J.G, t, bx * 32, by * (RPW * kRows), PJ ? J.cube : J.data,
+                                      PJ ? J.data : J.cube, acc, dsc);
 }
 
-template <int MODE, typename IDX, int RPW>
+template <int MODE, typename IDX, int RPW, bool DET>
 static void launch_packed_rpw(const long long *tile0, const PackedJob *jobs, int n_jobs, long long tiles, bool sun,
-                              cudaStream_t s) {
-  if (sun) packed_kernel<MODE, true, IDX, RPW><<<(unsigned)tiles, kThreads, 0, s>>>(tile0, jobs, n_jobs);
-  else packed_kernel<MODE, false, IDX, RPW><<<(unsigned)tiles, kThreads, 0, s>>>(tile0, jobs, n_jobs);
+                              unsigned char *ws, cudaStream_t s) {
+  if (sun) packed_kernel<MODE, true, IDX, RPW, DET><<<(unsigned)tiles, kThreads, 0, s>>>(tile0, jobs, n_jobs, ws);
+  else packed_kernel<MODE, false, IDX, RPW, DET><<<(unsigned)tiles, kThreads, 0, s>>>(tile0, jobs, n_jobs, ws);
 }
 
-template <int MODE, typename IDX>
+template <int MODE, typename IDX, bool DET = false>
 static void launch_packed_mode(const long long *tile0, const PackedJob *jobs, int n_jobs, long long tiles, int rpw,
-                               bool sun, cudaStream_t s) {
-  if (rpw == 1) launch_packed_rpw<MODE, IDX, 1>(tile0, jobs, n_jobs, tiles, sun, s);
-  else if (rpw == 2) launch_packed_rpw<MODE, IDX, 2>(tile0, jobs, n_jobs, tiles, sun, s);
-  else launch_packed_rpw<MODE, IDX, 4>(tile0, jobs, n_jobs, tiles, sun, s);
+                               bool sun, cudaStream_t s, unsigned char *ws = nullptr) {
+  if (rpw == 1) launch_packed_rpw<MODE, IDX, 1, DET>(tile0, jobs, n_jobs, tiles, sun, ws, s);
+  else if (rpw == 2) launch_packed_rpw<MODE, IDX, 2, DET>(tile0, jobs, n_jobs, tiles, sun, ws, s);
+  else launch_packed_rpw<MODE, IDX, 4, DET>(tile0, jobs, n_jobs, tiles, sun, ws, s);
+}
+
+// Deterministic packed backprojection, per job (blockIdx.y): max |y|, scale,
+// and the final scaled add of the accumulator into the job's cube.
+constexpr int kDetBlocks = 64;  // blocks per job of the prepass / finalize
+
+__global__ void packed_det_prepass(const PackedJob *__restrict__ jobs, unsigned char *__restrict__ ws) {
+  const PackedJob &J = jobs[blockIdx.y];
+  det_prepass_range(J.G, J.data, J.G.n_views, reinterpret_cast<DetScale *>(ws + J.ws_off),
+                    blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
+}
+
+__global__ void packed_det_scale(const PackedJob *__restrict__ jobs, int n_jobs, unsigned char *__restrict__ ws) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_jobs) return;
+  const PackedJob &J = jobs[k];
+  det_scale(reinterpret_cast<DetScale *>(ws + J.ws_off), J.rays, J.lmax);
+}
+
+__global__ void packed_det_finalize(const PackedJob *__restrict__ jobs, unsigned char *__restrict__ ws) {
+  const PackedJob &J = jobs[blockIdx.y];
+  det_finalize_range(J.G, reinterpret_cast<const long long *>(ws + J.ws_off + 256),
+                     reinterpret_cast<const DetScale *>(ws + J.ws_off), J.cube,
+                     blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
 }
 
 // byte offset of the job records in a plan of n_jobs jobs
@@ -92,9 +129,33 @@ cudaError_t launch_packed(const void *plan, int n_jobs, long long tiles, int rpw
   return cudaGetLastError();
 }
 
+cudaError_t launch_packed_det(const void *plan, int n_jobs, long long tiles, int rpw, bool idx64, bool four_d,
+                              int obstacle, void *workspace, size_t ws_bytes, cudaStream_t s) {
+  const long long *tile0 = (const long long *)plan;
+  const PackedJob *jobs = (const PackedJob *)((const unsigned char *)plan + packed_records_offset(n_jobs));
+  unsigned char *ws = (unsigned char *)workspace;
+  const bool sun = obstacle == TG_OBSTACLE_SUN;
+  cudaError_t e = cudaMemsetAsync(workspace, 0, ws_bytes, s);
+  if (e != cudaSuccess) return e;
+  packed_det_prepass<<<dim3(kDetBlocks, n_jobs), 256, 0, s>>>(jobs, ws);
+  packed_det_scale<<<(n_jobs + 127) / 128, 128, 0, s>>>(jobs, n_jobs, ws);
+  if (idx64) {
+    if (four_d) launch_packed_mode<TG_BPJT, long long, true>(tile0, jobs, n_jobs, tiles, rpw, sun, s, ws);
+    else launch_packed_mode<TG_BPJ, long long, true>(tile0, jobs, n_jobs, tiles, rpw, sun, s, ws);
+  } else {
+    if (four_d) launch_packed_mode<TG_BPJT, int, true>(tile0, jobs, n_jobs, tiles, rpw, sun, s, ws);
+    else launch_packed_mode<TG_BPJ, int, true>(tile0, jobs, n_jobs, tiles, rpw, sun, s, ws);
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  packed_det_finalize<<<dim3(kDetBlocks, n_jobs), 256, 0, s>>>(jobs, ws);
+  return cudaGetLastError();
+}
+
 size_t packed_job_bytes() { return sizeof(PackedJob); }
 
-void packed_fill(void *dst, const Geometry &G, float *data, float *cube, long long tile0, int gx, int gy) {
+void packed_fill(void *dst, const Geometry &G, float *data, float *cube, long long tile0, int gx, int gy,
+                 long long ws_off) {
   PackedJob *J = (PackedJob *)dst;
   J->G = G;
   J->data = data;
@@ -102,6 +163,10 @@ void packed_fill(void *dst, const Geometry &G, float *data, float *cube, long lo
   J->tile0 = tile0;
   J->gx = gx;
   J->gy = gy;
+  J->ws_off = ws_off;
+  det_acc_strides(G, J->acc_ms);
+  J->rays = (double)G.n1 * G.n2 * G.n_views;
+  J->lmax = det_lmax(G);
 }
 
 // ---------------------------------------------------------------------------

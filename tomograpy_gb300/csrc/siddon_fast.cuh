@@ -335,9 +335,11 @@ __device__ __forceinline__ bool setup_ray(const Geometry &G, const tg_image_head
       w.pa[k] = kInf;
       pl[k] = 0.f;
       dl[k] = 0.f;
+      df iaw = {0.f, 0.f};  // 1 / |w_k|, double-float
       if (w.upd[k]) {
         const df aw = (wd[k].hi > 0.f) ? wd[k] : df{-wd[k].hi, -wd[k].lo};
-        const df pd = df_mul({G.cdeltf[k], G.cdeltl[k]}, df_rcp(aw));
+        iaw = df_rcp(aw);
+        const df pd = df_mul({G.cdeltf[k], G.cdeltl[k]}, iaw);
         w.pa[k] = pd.hi;
         pl[k] = pd.lo;
       }
@@ -358,28 +360,41 @@ __device__ __forceinline__ bool setup_ray(const Geometry &G, const tg_image_head
         // cancellation of the two ~d-sized terms leaves ~1e-11 radii), then
         // the remainder against the exact plane position q * CDELT.
         const df e = df_add({T.mh[k], T.ml[k]}, df_mul(bin, wd[k]));
-        const float C = G.cdeltf[k];
+        const df C = {G.cdeltf[k], G.cdeltl[k]};
+        const df mC = {-C.hi, -C.lo};
         const float q = floorf((e.hi + e.lo) * G.inv_cdeltf[k]);
-        float r = fmaf(-q, C, e.hi) + fmaf(-q, G.cdeltl[k], e.lo);
+        // remainder r = e - q CDELT, kept in double-float: the distance to
+        // the next plane is r / |w|, and for a ray nearly parallel to the
+        // family (|w| ~ 1e-4 .. 1e-5) a float remainder (one ulp of CDELT,
+        // ~1e-9 radii) would shift that crossing by ~1e-5, which showed as
+        // per-voxel errors of 3e-4 on sparse backprojections
+        const df qc = df_mul({q, 0.f}, C);
+        df r = df_add(e, {-qc.hi, -qc.lo});
         int qi = (int)q;
-        if (r < 0.f) {
+        if (r.hi < 0.f || (r.hi == 0.f && r.lo < 0.f)) {
           qi -= 1;
-          r += C;
-        } else if (r >= C) {
-          qi += 1;
-          r -= C;
+          r = df_add(r, C);
+        } else {
+          const df rc = df_add(r, mC);
+          if (rc.hi > 0.f || (rc.hi == 0.f && rc.lo >= 0.f)) {
+            qi += 1;
+            r = rc;
+          }
         }
         // the reference truncates: a point just outside the first / last
         // voxel still maps to it (:785-786)
         if (qi == -1) {
           qi = 0;
-          r -= C;
+          r = df_add(r, mC);
         } else if (qi == G.n[k]) {
           qi = G.n[k] - 1;
-          r += C;
+          r = df_add(r, C);
         }
         iv[k] = qi;
-        w.d[k] = (w.upd[k] > 0) ? __fdiv_rn(C - r, w.uf[k]) : __fdiv_rn(r, -w.uf[k]);
+        // parameter of the first crossing: (CDELT - r) / w or r / -w
+        const df dd = df_mul((w.upd[k] > 0) ? df_add(C, {-r.hi, -r.lo}) : r, iaw);
+        w.d[k] = dd.hi;
+        dl[k] = dd.lo;
         ef[k] = e.hi + e.lo;
       }
     }

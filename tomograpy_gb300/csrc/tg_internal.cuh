@@ -80,7 +80,10 @@ cudaError_t launch_packed(const void *plan, int n_jobs, long long tiles, int rpw
                           cudaStream_t s);
 size_t packed_job_bytes();
 size_t packed_records_offset(int n_jobs);
-void packed_fill(void *dst, const Geometry &G, float *data, float *cube, long long tile0, int gx, int gy);
+void packed_fill(void *dst, const Geometry &G, float *data, float *cube, long long tile0, int gx, int gy,
+                 long long ws_off);
+cudaError_t launch_packed_det(const void *plan, int n_jobs, long long tiles, int rpw, bool idx64, bool four_d,
+                              int obstacle, void *workspace, size_t ws_bytes, cudaStream_t s);
 cudaError_t launch_seg_dot(const float *a, const float *b, const long long *off, int n_seg, double *partial,
                            double *out, cudaStream_t st);
 cudaError_t launch_seg_cg_x(float *x, float *r, const float *p, const float *Ap, const double *rr, const double *pAp,

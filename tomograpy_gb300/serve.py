@@ -141,10 +141,15 @@ class Server:
     iterations past its tolerance)."""
 
     def __init__(self, budget_bytes=None, lam=1e-2, obstacle="sun", rows_per_warp=4, device=None,
-                 cube_fraction=0.4, max_rays=1 << 23, max_wait=1.0, max_slots=4096):
+                 cube_fraction=0.4, max_rays=1 << 23, max_wait=1.0, max_slots=4096, deterministic=False):
         self.L = B._bind(_lib.load())
         self.dev = device or S._device()
         self.lam = float(lam)
+        # fixed-point backprojections: a request's result is then bitwise the
+        # same alone, in any mix, and in the plain loop with a deterministic
+        # operator (see batch.batched_cg)
+        self.deterministic = bool(deterministic)
+        self._ws = None
         self.obstacle = obstacle
         self.rpw = rows_per_warp
         self.max_rays = int(max_rays)
@@ -182,6 +187,21 @@ class Server:
         self.host_s = {"admit": 0.0, "rebuild": 0.0, "step": 0.0, "retire": 0.0, "wait": 0.0, "collect": 0.0}
         self.rebuilds = 0
 
+    def _workspace(self, nbytes):
+        """Deterministic-backprojection workspace (grown, never shrunk)."""
+        if self._ws is None or self._ws.numel() < nbytes:
+            self._ws = torch.empty(max(int(nbytes), 2 * (0 if self._ws is None else self._ws.numel())),
+                                   dtype=torch.uint8, device=self.dev)
+        return self._ws
+
+    def _bpj_single(self, dv, cube, views, mh, T):
+        if self.deterministic:
+            need = self.L.tg_deterministic_workspace_bytes(_lib.i64(list(cube.shape) + [1]))
+            S.run_device("bpj", dv, cube, views, mh, T, obstacle=self.obstacle, deterministic=True,
+                         workspace=self._workspace(need))
+        else:
+            S.run_device("bpj", dv, cube, views, mh, T, obstacle=self.obstacle)
+
     # admission -------------------------------------------------------------
     def try_admit(self, req):
         nc = int(np.prod(req.job.cube_shape))
@@ -207,7 +227,7 @@ class Server:
         r.zero_()
         mh = S.pack_map_header(req.job.cube_header)
         job.mh = mh
-        S.run_device("bpj", dv, r.view(*req.job.cube_shape), views, mh, T, obstacle=self.obstacle)
+        self._bpj_single(dv, r.view(*req.job.cube_shape), views, mh, T)
         self.vec["p"][c[0]:c[0] + nc].copy_(r)
         self.vec["x"][c[0]:c[0] + nc].zero_()
         rd = r.double()
@@ -286,14 +306,18 @@ class Server:
             S.run_device("pj", dv, v["p"][job.c[0]:job.c[0] + job.nc].view(*shape), job.views, job.mh, T,
                          obstacle=self.obstacle)
             ops.axpby(v["a"], None, 0.0, 0.0)
-            S.run_device("bpj", dv, v["a"][job.c[0]:job.c[0] + job.nc].view(*shape), job.views, job.mh, T,
-                         obstacle=self.obstacle)
+            self._bpj_single(dv, v["a"][job.c[0]:job.c[0] + job.nc].view(*shape), job.views, job.mh, T)
         else:
             buf, info = self.plans["pj"]
             _lib.check(L.tg_packed_projector(B._ptr(buf), ctypes.byref(info), _lib.TG_PJ, ob, st))   # P p
             ops.axpby(v["a"], None, 0.0, 0.0)
             buf, info = self.plans["bpj"]
-            _lib.check(L.tg_packed_projector(B._ptr(buf), ctypes.byref(info), _lib.TG_BPJ, ob, st))  # P^T P p
+            if self.deterministic:                                                                    # P^T P p
+                ws = self._workspace(info.det_workspace_bytes)
+                _lib.check(L.tg_packed_backprojector_deterministic(B._ptr(buf), ctypes.byref(info), ob, B._ptr(ws),
+                                                                   ws.numel(), st))
+            else:
+                _lib.check(L.tg_packed_projector(B._ptr(buf), ctypes.byref(info), _lib.TG_BPJ, ob, st))
         if self.lam:
             ops.axpby(v["a"], v["p"], self.lam, 1.0)
         ops.dot(v["p"], v["a"], self.pAp)
@@ -436,7 +460,7 @@ def summarize(done, wall, iterations):
             "max_residual": float(max(r.residual for r in done))}
 
 
-def fifo_plain(requests, lam=1e-2, obstacle="sun", device=None):
+def fifo_plain(requests, lam=1e-2, obstacle="sun", device=None, deterministic=False):
     """Baseline: requests served one at a time in arrival order with the plain
     single-job operator and CG (stopping at the same tolerance / budget)."""
     from . import cg, lo_wrapper
@@ -448,7 +472,7 @@ def fifo_plain(requests, lam=1e-2, obstacle="sun", device=None):
         if req.arrival > now:
             time.sleep(req.arrival - now)
         op = lo_wrapper.siddon_lo(req.job.view_headers, req.job.cube_header, obstacle=obstacle, dtype=np.float32,
-                                  device=dev)
+                                  device=dev, deterministic=deterministic)
         host = req.data if torch.is_tensor(req.data) else torch.from_numpy(np.ascontiguousarray(req.data))
         b = op.backproject(host.to(dev))
         res = cg.cg(cg.NormalOperator(op, lam=lam), b, maxiter=req.max_iters, tol=req.tol)

@@ -52,13 +52,14 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-other", action="store_true", help=argparse.SUPPRESS)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the uneven multi-job batch measurement")
     ap.add_argument("--no-served", action="store_true", help="skip the serving-stream measurement")
     ap.add_argument("--no-4d", action="store_true", help="skip the time-dependent (4-D) measurement")
     ap.add_argument("--no-lbfgs", action="store_true", help="skip the differentiable-reconstruction measurement")
-    ap.add_argument("--served-jobs", type=int, default=60,
-                    help="requests of the serving stream sample (Poisson, 20 jobs/s)")
+    ap.add_argument("--served-jobs", type=int, default=2000,
+                    help="requests of the serving stream (Poisson, 20 jobs/s)")
     ap.add_argument("--profile-packed", action="store_true",
                     help="one packed projection + backprojection of the 32-job uneven batch (the case of the "
                          "packed-kernel ncu summary in profiles/)")
@@ -168,66 +169,169 @@ def ncu_traffic(kernel):
 
 
 # ---------------------------------------------------------------------------
-# CPU baseline: the oracle (C restatement of the reference's OpenMP kernel)
+# CPU baseline: the oracle (C restatement of the reference's OpenMP kernel).
+# One method everywhere: after an untimed warm-up run, a timing is the best of
+# several runs of one projection + one backprojection of the sample on all
+# host threads, float32 (the benchmark's precision) unless stated; float64
+# (the reference's precision of record) is timed beside it.  The bench line's
+# cpu_baseline is the reference arm itself, run in a fresh process.
 
+CPU_REPEATS = 3
 _CPU_CACHE = {}
 
 
-def cpu_sample(n_views=CPU_SAMPLE_VIEWS, threads=None, repeats=1):
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_model():
+    """Host CPU model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
+
+
+def _cpu_geometry(name):
+    import numpy as np
+
+    from tomograpy_gb300 import synthetic
+    if name not in _CPU_CACHE:
+        ch, vh = synthetic.make_geometry(name)
+        if name == "frames128":
+            cfg = synthetic.CONFIGS[name]
+            x = synthetic.phantom4d(ch, cfg["n_frames"], seed=0)
+        else:
+            x = synthetic.phantom(ch, seed=0)
+        _CPU_CACHE[name] = (ch, vh, np.ascontiguousarray(x))
+    return _CPU_CACHE[name]
+
+
+def _cpu_pair(ch, vh, x, dtype, threads):
+    """Seconds of one oracle projection + backprojection of views vh."""
     import numpy as np
 
     import oracle
-    from tomograpy_gb300 import synthetic
     from tomograpy_gb300.infoarray import InfoArray
-    cfg = synthetic.CONFIGS[WORKLOAD]
-    if "geom" not in _CPU_CACHE:
-        ch, vh = synthetic.make_geometry(WORKLOAD)
-        _CPU_CACHE["geom"] = (ch, vh, synthetic.phantom(ch, seed=0))
-    ch, vh, x = _CPU_CACHE["geom"]
-    idx = np.linspace(0, cfg["T"] - 1, n_views).round().astype(int)
-    sub = [dict(vh[i]) for i in idx]
-    threads = threads or os.cpu_count()
+    N1, N2 = int(vh[0]["NAXIS1"]), int(vh[0]["NAXIS2"])
+    data = InfoArray(shape=(N1, N2, len(vh)), header=[dict(h) for h in vh], dtype=dtype)
+    cube = InfoArray(data=x.astype(dtype), header=dict(ch))
+    bcube = InfoArray(shape=x.shape, header=dict(ch), dtype=dtype)
+    t0 = time.perf_counter()
+    oracle.projector(data, cube, obstacle="sun", nthread=threads)
+    oracle.backprojector(data, bcube, obstacle="sun", nthread=threads)
+    return time.perf_counter() - t0
+
+
+def cpu_time(name, dtype="float32", n_views=None, threads=None, repeats=CPU_REPEATS):
+    """(best seconds, rays) of the pj + bpj pair of workload ``name`` on the
+    oracle: every view, or ``n_views`` of them spread over the orbit.  The
+    time-dependent workload runs frame by frame (each frame's views against
+    its own 3-D cube: the same rays and voxels as the 4-D call)."""
+    import numpy as np
+    threads = threads or host_threads()
+    ch, vh, x = _cpu_geometry(name)
+    if n_views is not None:
+        idx = np.linspace(0, len(vh) - 1, n_views).round().astype(int)
+        vh = [vh[i] for i in idx]
+    rays = int(vh[0]["NAXIS1"]) * int(vh[0]["NAXIS2"]) * len(vh)
     best = None
     for _ in range(repeats):
-        data = InfoArray(shape=(cfg["N"], cfg["N"], n_views), header=sub, dtype=np.float32)
-        cube = InfoArray(data=x, header=dict(ch))
-        t0 = time.perf_counter()
-        oracle.projector(data, cube, obstacle="sun", nthread=threads)
-        bcube = InfoArray(shape=x.shape, header=dict(ch), dtype=np.float32)
-        oracle.backprojector(data, bcube, obstacle="sun", nthread=threads)
-        dt = time.perf_counter() - t0
+        if x.ndim == 4:
+            F = x.shape[3]
+            per = len(vh) // F
+            ch3 = dict(ch, NAXIS=3)
+            dt = sum(_cpu_pair(ch3, vh[f * per:(f + 1) * per], x[..., f], dtype, threads) for f in range(F))
+        else:
+            dt = _cpu_pair(ch, vh, x, dtype, threads)
         best = dt if best is None else min(best, dt)
-    rays = cfg["N"] * cfg["N"] * n_views
-    return rays / best, best, threads, rays
+    return best, rays
 
 
-def cpu_baseline_entry(value, threads, sample):
-    return {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}
+def cpu_other(threads):
+    """CPU timings beside the headline baseline: the float64 sample of the
+    headline workload and the full-size plain (64^3 x 60 x 128^2) and
+    time-dependent (128^3 x 28 frames, 784 x 256^2) workloads, float32 and
+    float64 (one untimed warm-up run each, then the best of the repeats)."""
+    other = {}
+    cpu_time(WORKLOAD, "float64", CPU_SAMPLE_VIEWS, threads, repeats=1)
+    dt64, rays = cpu_time(WORKLOAD, "float64", CPU_SAMPLE_VIEWS, threads)
+    other["recon256_sample_f64"] = {"value": rays / dt64, "unit": UNIT, "seconds": dt64, "rays": rays,
+                                    "repeats": CPU_REPEATS}
+    for name, reps in (("plain64", CPU_REPEATS), ("frames128", 1)):
+        for dtype in ("float32", "float64"):
+            cpu_time(name, dtype, None, threads, repeats=1)
+            t, r = cpu_time(name, dtype, None, threads, repeats=reps)
+            other["%s_full_%s" % (name, "f32" if dtype == "float32" else "f64")] = {
+                "value": r / t, "unit": UNIT, "seconds": t, "rays": r, "repeats": reps}
+    return other
+
+
+def _bench_subprocess(extra):
+    """Run this script in a fresh process (no CUDA context, nothing else on
+    the host threads) and return its last JSON line."""
+    out = subprocess.run([sys.executable, os.path.abspath(__file__)] + extra, capture_output=True, text=True,
+                         env=dict(os.environ, RANK="0", WORLD_SIZE="1"), timeout=1800)
+    lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
+    if out.returncode != 0 or not lines:
+        raise RuntimeError("CPU baseline subprocess failed: %s" % out.stderr[-500:])
+    return json.loads(lines[-1])
+
+
+def cpu_baseline(args):
+    """The bench line's CPU baseline: exactly the reference arm
+    (``--impl reference`` with the same --steps / --warmup, in a fresh
+    process), so the two agree by construction, plus cpu_other()."""
+    ref = _bench_subprocess(["--impl", "reference", "--steps", str(args.steps), "--warmup", str(args.warmup)])
+    entry = dict(ref["cpu_baseline"])
+    entry["ms_per_step"] = ref["ms_per_step"]
+    entry["other"] = _bench_subprocess(["--cpu-other"])
+    return entry
 
 
 def run_reference(args):
+    """The reference algorithm's CPU path (the oracle port, float32, all host
+    threads): each step is one projection + backprojection of the fixed
+    16-view sample of the headline workload; the value is the best step,
+    the same method as the bench line's cpu_baseline."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    threads = os.cpu_count()
+    threads = host_threads()
+    for _ in range(max(1, args.warmup)):
+        cpu_time(WORKLOAD, "float32", CPU_SAMPLE_VIEWS, threads, repeats=1)
     times = []
-    for _ in range(args.warmup):
-        cpu_sample(threads=threads)
     rays = None
     for _ in range(args.steps):
-        _, dt, threads, rays = cpu_sample(threads=threads)
+        dt, rays = cpu_time(WORKLOAD, "float32", CPU_SAMPLE_VIEWS, threads, repeats=1)
         times.append(dt)
-    ms = 1000.0 * statistics.mean(times)
-    value = rays / (ms / 1000.0)
+    best = min(times)
+    value = rays / best
     sample = ("oracle float32 (C/OpenMP restatement of tomograpy/C_siddon.c.template), %d of 360 views "
-              "(%d rays) per step, projection + backprojection, %d threads" % (CPU_SAMPLE_VIEWS, rays, threads))
+              "(%d rays) per step, projection + backprojection, best of %d steps, %d threads of %s"
+              % (CPU_SAMPLE_VIEWS, rays, args.steps, threads, cpu_model()))
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * best,
+        "ms_per_step_mean": 1000.0 * statistics.mean(times), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "description": WORKLOAD_DESC, "sample_views": CPU_SAMPLE_VIEWS,
                    "parallelism": "host threads (OpenMP over views)"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                         "cpu_model": cpu_model()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
 
@@ -248,10 +352,7 @@ def run_ours(args):
     # CPU baseline first (host threads only; no GPU context yet)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        v, dt, threads, rays = cpu_sample(threads=os.cpu_count(), repeats=2)
-        cpu = cpu_baseline_entry(v, threads, "oracle float32 (C/OpenMP restatement of the reference kernel), "
-                                             "%d of 360 views (%d rays), projection + backprojection, %.1f s"
-                                 % (CPU_SAMPLE_VIEWS, rays, dt))
+        cpu = guarded(cpu_baseline, args)
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     cfg = synthetic.CONFIGS[WORKLOAD]
@@ -357,14 +458,16 @@ def run_ours(args):
         lbfgs = guarded(measure_lbfgs, dev)
     if rank == 0 and not args.no_4d:
         four_d = guarded(measure_4d, dev)
+    full_rate = inter / (ms / 1000.0)   # segments per second through a pj + bpj pair, fully loaded
     if rank == 0 and not args.no_batched:
-        batched = guarded(measure_batched, dev)
+        batched = guarded(measure_batched, dev, full_rate=full_rate)
         if "error" not in batched:
-            batched["small_jobs"] = guarded(measure_batched, dev, n_jobs=256, mix=SMALL_MIX)
+            batched["small_jobs"] = guarded(measure_batched, dev, n_jobs=256, mix=SMALL_MIX, full_rate=full_rate)
     if rank == 0 and not args.no_served:
-        served = guarded(measure_served, dev, args.served_jobs)
+        served = guarded(measure_served, dev, args.served_jobs, full_rate=full_rate)
         if "error" not in served:
-            served["small_jobs"] = guarded(measure_served, dev, 500, rate=4000.0, mix=SMALL_MIX, large=0.0)
+            served["small_jobs"] = guarded(measure_served, dev, 500, rate=4000.0, mix=SMALL_MIX, large=0.0,
+                                           pool=500, full_rate=full_rate)
 
     if rank == 0:
         out = {
@@ -448,7 +551,7 @@ def deterministic_bpj_ms(y, c, views, mh, T, n, flush, e, reps=3):
     return statistics.mean(ts)
 
 
-def measure_lbfgs(dev, iters=10):
+def measure_lbfgs(dev, iters=50):
     """Differentiable reconstruction on the benchmark geometry: L-BFGS on
     0.5 |P x - y|^2 / |y|^2 + 1e-3 TV_eps(x) with x = s softplus(z), the
     projector as a torch.autograd.Function whose backward is the
@@ -533,13 +636,29 @@ SERVE_BUDGET = 48 << 30   # device memory the serving measurement may keep resid
 SMALL_MIX = dict(edges=(16, 24, 32, 48), sides=(32, 48, 64), views=(8, 32))
 
 
-def measure_batched(dev, n_jobs=32, iters=20, seed=0, mix=None):
+def job_segments(job, dev):
+    """Voxel segments one projection of a job traces (the exact count)."""
+    import torch
+
+    from tomograpy_gb300 import siddon
+    n1, n2, T = job.data_shape
+    views = siddon.upload_views(job.view_headers, job.frames, dev)
+    c = siddon.segment_counts(views, siddon.pack_map_header(job.cube_header), job.cube_shape[:3], n1, n2, T,
+                              obstacle="sun")
+    return float(c.sum(dtype=torch.float64))
+
+
+def measure_batched(dev, n_jobs=32, iters=20, seed=0, mix=None, full_rate=None):
     """Uneven multi-job batch: 32 seeded reconstructions (cube edge in
     {32..192}, 16-256 views of 64-512 px, d in [150, 230]; or the sizes of
     `mix`), 20 CG iterations on (P^T P + 1e-2 I) x = P^T y each, solved (a)
     together with one packed launch per direction per iteration, CUDA-graph
     captured, tile shape autotuned, and (b) one after another with the
-    single-job operator."""
+    single-job operator.  Also: the same with fixed-point backprojections
+    (every job's iterate then bitwise the plain loop's), and the ceiling of
+    any batching: plain time / the time of the batch's voxel segments at the
+    fully loaded rate of the headline workload (``full_rate``, segments per
+    second through a projection + backprojection pair)."""
     import torch
 
     from tomograpy_gb300 import batch, synthetic
@@ -565,49 +684,119 @@ def measure_batched(dev, n_jobs=32, iters=20, seed=0, mix=None):
     ts = time.perf_counter() - t0
     diff = max(float((pack.cube_view(xb, k) - xs[k]).abs().max() / xs[k].abs().max().clamp_min(1e-30))
                for k in range(n_jobs))
+    # deterministic mode: bitwise isolation at the full iteration count
+    batch.batched_cg(pack, b, iters=2, deterministic=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    xd, _ = batch.batched_cg(pack, b, iters=iters, deterministic=True)
+    torch.cuda.synchronize()
+    tbd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    xsd = batch.sequential_cg(jobs, rhs, iters=iters, deterministic=True)
+    torch.cuda.synchronize()
+    tsd = time.perf_counter() - t0
+    bitwise = all(torch.equal(pack.cube_view(xd, k), xsd[k]) for k in range(n_jobs))
     rays = sum(int(j.data_shape[0] * j.data_shape[1] * j.data_shape[2]) for j in jobs)
+    out = {"rays_per_iteration": rays, "rows_per_warp": pack.rows_per_warp,
+           "batched_cg_it_per_s": n_jobs * iters / tb, "plain_cg_it_per_s": n_jobs * iters / ts,
+           "speedup": ts / tb, "batched_s": tb, "plain_s": ts, "max_rel_diff_vs_plain": diff,
+           "deterministic": {"batched_cg_it_per_s": n_jobs * iters / tbd, "plain_cg_it_per_s": n_jobs * iters / tsd,
+                             "speedup": tsd / tbd, "bitwise_equal_to_plain": bitwise},
+           "plain": "one job after another: single-job operator + the same CG kernels (no graph)"}
+    if full_rate:
+        segs = sum(job_segments(j, dev) for j in jobs)
+        t_lb = iters * segs / full_rate
+        out["ceiling"] = {"segments_per_iteration": segs, "lower_bound_s": t_lb, "speedup_ceiling": ts / t_lb,
+                          "how": "plain time / (iterations x segments / fully loaded segment rate of the "
+                                 "headline projection + backprojection pair)"}
     sizes = ("edges %s, %d-%d views, %s px" % (mix["edges"], mix["views"][0], mix["views"][1], mix["sides"])
              if mix else "edges 32-192, 16-256 views, 64-512 px")
-    return {"workload": "uneven batch: %d seeded jobs (%s), %d CG iterations, sun" % (n_jobs, sizes, iters),
-            "rays_per_iteration": rays, "rows_per_warp": pack.rows_per_warp,
-            "batched_cg_it_per_s": n_jobs * iters / tb, "plain_cg_it_per_s": n_jobs * iters / ts,
-            "speedup": ts / tb, "batched_s": tb, "plain_s": ts, "max_rel_diff_vs_plain": diff,
-            "plain": "one job after another: single-job operator + the same CG kernels (no graph)"}
+    out["workload"] = "uneven batch: %d seeded jobs (%s), %d CG iterations, sun" % (n_jobs, sizes, iters)
+    return out
 
 
-def measure_served(dev, n_jobs=60, rate=20.0, seed=0, mix=None, large=0.1):
-    """Serving stream sample: Poisson arrivals (20 jobs/s, seeded), sizes as the
-    uneven batch (or `mix`) plus a fraction `large` of 256^3 x 360 x 512^2
-    jobs, 20 CG iterations or relative residual 1e-4 each; continuous
-    batching vs a FIFO plain loop."""
+def serving_payloads(dev, seed, mix, large, pool):
+    """The stream's distinct request payloads (geometry + pinned host data
+    stack P(phantom)): ``pool`` seeded draws of the uneven-batch sizes (or
+    ``mix``), plus one 256^3 x 360 x 512^2 job when ``large`` > 0."""
+    from tomograpy_gb300 import serve, synthetic
+    specs = synthetic.uneven_specs(pool, seed=seed + 1, **(mix or {}))
+    small = serve.poisson_requests(specs, rate=1.0, seed=seed, max_iters=20, tol=1e-4, device=dev)
+    big = None
+    if large > 0:
+        big = serve.poisson_requests([dict(synthetic.CONFIGS["recon256"])], rate=1.0, seed=seed, max_iters=20,
+                                     tol=1e-4, device=dev)[0]
+    return small, big
+
+
+def serving_requests(dev, n_jobs, rate, seed, mix, large, pool, payloads=None):
+    """Poisson arrivals of ``n_jobs`` requests at ``rate`` jobs/s (seeded).
+    Sizes: a fraction ``large`` of 256^3 x 360 x 512^2 jobs, the others drawn
+    from ``pool`` seeded draws of the uneven-batch distribution (or ``mix``);
+    requests that draw the same entry share its geometry and host data stack,
+    which keeps the stream's host memory bounded."""
     import numpy as np
 
-    from tomograpy_gb300 import serve, synthetic
+    from tomograpy_gb300 import serve
+    small, big = payloads or serving_payloads(dev, seed, mix, large, pool)
     rng = np.random.default_rng(seed + 99)
-    specs = synthetic.uneven_specs(n_jobs, seed=seed + 1, **(mix or {}))
+    t = 0.0
+    reqs = []
     for k in range(n_jobs):
-        if rng.random() < large:
-            specs[k] = dict(synthetic.CONFIGS["recon256"])
+        t += rng.exponential(1.0 / rate)
+        src = big if (big is not None and rng.random() < large) else small[int(rng.integers(pool))]
+        reqs.append(serve.Request(k, src.job, src.data, t, max_iters=20, tol=1e-4))
+    return reqs, (small, big)
+
+
+def measure_served(dev, n_jobs=2000, rate=20.0, seed=0, mix=None, large=0.1, pool=64, full_rate=None):
+    """Serving stream: Poisson arrivals (20 jobs/s, seeded) of requests sized
+    as the uneven batch (or `mix`) plus a fraction `large` of 256^3 x 360 x
+    512^2 jobs, 20 CG iterations or relative residual 1e-4 each; continuous
+    batching vs a FIFO plain loop on the same requests."""
+    import numpy as np
+
+    from tomograpy_gb300 import serve
     # warm-up (untimed): the first launches of every kernel variant and the
     # first pinned allocations of a process would otherwise land in the stream
-    warm = serve.poisson_requests(specs[:8], rate=1e6, seed=seed, max_iters=3, tol=1e-4, device=dev)
+    warm, _ = serving_requests(dev, 8, 1e6, seed, mix, 0.0, min(pool, 8))
+    for r in warm:
+        r.max_iters = 3
     serve.Server(budget_bytes=8 << 30, device=dev).run(warm)
-    serve.fifo_plain(serve.poisson_requests(specs[:8], rate=1e6, seed=seed, max_iters=3, tol=1e-4, device=dev),
-                     device=dev)
-    reqs = serve.poisson_requests(specs, rate=rate, seed=seed, max_iters=20, tol=1e-4, device=dev)
-    srv = serve.Server(budget_bytes=SERVE_BUDGET, device=dev)
+    warm, _ = serving_requests(dev, 8, 1e6, seed, mix, 0.0, min(pool, 8))
+    for r in warm:
+        r.max_iters = 3
+    serve.fifo_plain(warm, device=dev)
+    # results are delivered to the host for every request; every 20th is kept
+    # for the comparison of the two arms (bounded host memory)
+    keep = set(range(0, n_jobs, 20))
+
+    def done(r):
+        if r.id not in keep:
+            r.result = None
+    reqs, payloads = serving_requests(dev, n_jobs, rate, seed, mix, large, pool)
+    srv = serve.Server(budget_bytes=SERVE_BUDGET, device=dev, on_done=done)
     s = srv.run(reqs)
-    reqs2 = serve.poisson_requests(specs, rate=rate, seed=seed, max_iters=20, tol=1e-4, device=dev)
-    f = serve.fifo_plain(reqs2, device=dev)
-    diff = max(float((a.result - c.result).abs().max() / c.result.abs().max().clamp_min(1e-30))
-               for a, c in zip(reqs, reqs2))
+    reqs2, _ = serving_requests(dev, n_jobs, rate, seed, mix, large, pool, payloads)
+    f = serve.fifo_plain(reqs2, device=dev, on_done=done)
+    diff = max(float((reqs[k].result - reqs2[k].result).abs().max() /
+                     reqs2[k].result.abs().max().clamp_min(1e-30)) for k in sorted(keep))
+    out = {"served": s, "fifo_plain": f, "cg_it_per_s_ratio": s["cg_it_per_s"] / f["cg_it_per_s"],
+           "p99_ratio": s["p99_s"] / f["p99_s"], "max_inflight": srv.max_inflight, "max_rel_diff_vs_plain": diff,
+           "budget_bytes": SERVE_BUDGET, "server_host_s": srv.host_s, "server_rebuilds": srv.rebuilds,
+           "large_requests": int(sum(r.job is payloads[1].job for r in reqs)) if large > 0 else 0}
+    if full_rate:
+        segs = {id(p.job): job_segments(p.job, dev) for p in payloads[0] + ([payloads[1]] if payloads[1] else [])}
+        t_lb = sum(r.iters * segs[id(r.job)] for r in reqs2) / full_rate
+        out["ceiling"] = {"lower_bound_s": t_lb, "cg_it_per_s_ceiling": f["wall_s"] / t_lb,
+                          "how": "FIFO wall time / (the FIFO jobs' iterations x segments at the fully loaded "
+                                 "segment rate of the headline pair); meaningful when arrivals outpace the GPU"}
     sizes = ("small uneven sizes (edges %s, %d-%d views, %s px)" % (mix["edges"], mix["views"][0], mix["views"][1],
                                                                       mix["sides"]) if mix else "uneven sizes")
-    return {"workload": "serving stream: %d Poisson requests at %.0f jobs/s, %s + %d%% 256^3 x 360 x 512^2, "
-                        "20 CG iterations or residual 1e-4" % (n_jobs, rate, sizes, round(100 * large)),
-            "served": s, "fifo_plain": f, "cg_it_per_s_ratio": s["cg_it_per_s"] / f["cg_it_per_s"],
-            "max_inflight": srv.max_inflight, "max_rel_diff_vs_plain": diff, "budget_bytes": SERVE_BUDGET,
-            "server_host_s": srv.host_s, "server_rebuilds": srv.rebuilds}
+    out["workload"] = ("serving stream: %d Poisson requests at %.0f jobs/s, %s from %d seeded draws + %d%% "
+                       "256^3 x 360 x 512^2, 20 CG iterations or residual 1e-4" % (n_jobs, rate, sizes, pool,
+                                                                                  round(100 * large)))
+    return out
 
 
 def run_profile_case():
@@ -653,6 +842,9 @@ def main():
         return
     if args.profile_packed:
         run_profile_packed()
+        return
+    if args.cpu_other:
+        print(json.dumps(cpu_other(host_threads())))
         return
     if args.impl == "reference":
         run_reference(args)

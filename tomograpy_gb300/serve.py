@@ -141,7 +141,8 @@ class Server:
     iterations past its tolerance)."""
 
     def __init__(self, budget_bytes=None, lam=1e-2, obstacle="sun", rows_per_warp=4, device=None,
-                 cube_fraction=0.4, max_rays=1 << 23, max_wait=1.0, max_slots=4096, deterministic=False):
+                 cube_fraction=0.4, max_rays=1 << 23, max_wait=1.0, max_slots=4096, deterministic=False,
+                 on_done=None):
         self.L = B._bind(_lib.load())
         self.dev = device or S._device()
         self.lam = float(lam)
@@ -150,6 +151,7 @@ class Server:
         # operator (see batch.batched_cg)
         self.deterministic = bool(deterministic)
         self._ws = None
+        self.on_done = on_done   # called with each request once its result is on the host
         self.obstacle = obstacle
         self.rpw = rows_per_warp
         self.max_rays = int(max_rays)
@@ -386,6 +388,8 @@ class Server:
             if req.residual is None:
                 req.residual = float("nan")
             self.completed.append(req)
+            if self.on_done is not None:
+                self.on_done(req)
 
     def _rays_inflight(self):
         return sum(job.nd for job in self.inflight)
@@ -393,17 +397,23 @@ class Server:
     def _admit(self, queue, now):
         """Admit queued requests while the in-flight rays stay under
         ``max_rays`` (one step is then a few tens of waves of the GPU) and
-        memory allows.  Candidates are taken shortest job first (fewest rays:
-        a small request is not held behind a large one), except that a
-        request waiting longer than ``max_wait`` seconds goes first and, if it
-        does not fit, stops further admissions until the server drains enough
-        for it; an empty server always admits its first candidate."""
+        memory allows.  Requests that have waited at least ``max_wait``
+        seconds go first, oldest first, and the first of them that does not
+        fit stops further admissions until the server has drained enough for
+        it (so no request waits behind a stream of later ones); the others
+        follow shortest job first (fewest rays: a small request is not held
+        behind a large one).  An empty server always admits its first
+        candidate."""
         if not queue:
             return
         rays = self._rays_inflight()
-        order = sorted(range(len(queue)),
-                       key=lambda k: (now - queue[k].arrival < self.max_wait, int(np.prod(queue[k].job.data_shape)),
-                                      queue[k].arrival))
+
+        def key(k):
+            q = queue[k]
+            if now - q.arrival >= self.max_wait:
+                return (0, q.arrival, 0)
+            return (1, int(np.prod(q.job.data_shape)), q.arrival)
+        order = sorted(range(len(queue)), key=key)
         admitted = set()
         for k in order:
             req = queue[k]
@@ -460,9 +470,10 @@ def summarize(done, wall, iterations):
             "max_residual": float(max(r.residual for r in done))}
 
 
-def fifo_plain(requests, lam=1e-2, obstacle="sun", device=None, deterministic=False):
+def fifo_plain(requests, lam=1e-2, obstacle="sun", device=None, deterministic=False, on_done=None):
     """Baseline: requests served one at a time in arrival order with the plain
-    single-job operator and CG (stopping at the same tolerance / budget)."""
+    single-job operator and CG (stopping at the same tolerance / budget).
+    ``on_done`` is called with each request once its result is on the host."""
     from . import cg, lo_wrapper
     dev = device or S._device()
     t_start = time.perf_counter()
@@ -481,6 +492,8 @@ def fifo_plain(requests, lam=1e-2, obstacle="sun", device=None, deterministic=Fa
         req.iters = res.iterations
         iterations += res.iterations
         req.t_done = time.perf_counter() - t_start
+        if on_done is not None:
+            on_done(req)
     torch.cuda.synchronize()
     return summarize(list(requests), time.perf_counter() - t_start, iterations)
 

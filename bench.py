@@ -697,7 +697,15 @@ def measure_batched(dev, n_jobs=32, iters=20, seed=0, mix=None, full_rate=None):
     tsd = time.perf_counter() - t0
     bitwise = all(torch.equal(pack.cube_view(xd, k), xsd[k]) for k in range(n_jobs))
     rays = sum(int(j.data_shape[0] * j.data_shape[1] * j.data_shape[2]) for j in jobs)
+    table = pack.tune_table or {}
+    default = batch.DEFAULT_SCHEDULE
     out = {"rays_per_iteration": rays, "rows_per_warp": pack.rows_per_warp,
+           "schedule": {"rows_per_warp": pack.schedule[0], "lane_axis": "lambda" if pack.schedule[1] else "gamma",
+                        "batch_steps": pack.schedule[2] or "default",
+                        "autotune_s_per_pj_bpj": {"%d/%s/%s" % (k[0], "lambda" if k[1] else "gamma", k[2] or "default"):
+                                                  v for k, v in table.items()},
+                        "gain_over_default": (table[default] / table[pack.schedule]
+                                              if default in table and pack.schedule in table else None)},
            "batched_cg_it_per_s": n_jobs * iters / tb, "plain_cg_it_per_s": n_jobs * iters / ts,
            "speedup": ts / tb, "batched_s": tb, "plain_s": ts, "max_rel_diff_vs_plain": diff,
            "deterministic": {"batched_cg_it_per_s": n_jobs * iters / tbd, "plain_cg_it_per_s": n_jobs * iters / tsd,

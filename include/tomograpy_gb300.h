@@ -223,8 +223,25 @@ typedef struct {
   int64_t tiles;                 /* CTAs of one packed launch */
   int64_t det_workspace_bytes;   /* workspace of tg_packed_backprojector_deterministic */
   int32_t det_idx64;             /* a job's accumulator needs 64-bit offsets */
+  int32_t lane_axis;             /* schedule of the plan (see tg_schedule) */
+  int32_t batch_steps;
   int32_t reserved;
 } tg_packed_info;
+
+/* Tile schedule of a packed plan (picked by timing, see
+ * tomograpy_gb300/batch.py): rows_per_warp 1, 2 or 4; lane_axis 1 = a warp's
+ * 32 lanes trace neighbouring pixels along image axis 1 (lambda; tiles of
+ * 8*rows_per_warp rows x 32 columns), 0 = along image axis 0 (gamma; tiles of
+ * 32 rows x 8*rows_per_warp columns), the better mapping when image axis 0
+ * follows the cube's fastest axis; batch_steps 0 = the default walk batches,
+ * 16 = 16-step batches.  Plans whose cube offsets need 64 bits always use
+ * lane_axis 1, batch_steps 0 (info reports the schedule used). */
+typedef struct {
+  int32_t rows_per_warp;
+  int32_t lane_axis;
+  int32_t batch_steps;
+  int32_t reserved;
+} tg_schedule;
 
 size_t tg_packed_plan_bytes(int32_t n_jobs);
 tg_status tg_packed_plan(const tg_job *jobs, int32_t n_jobs, int32_t rows_per_warp, int32_t four_d, void *plan,
@@ -234,6 +251,12 @@ tg_status tg_packed_plan(const tg_job *jobs, int32_t n_jobs, int32_t rows_per_wa
  * stream, so re-planning does not stall a stream that is busy. */
 tg_status tg_packed_plan_host(const tg_job *jobs, int32_t n_jobs, int32_t rows_per_warp, int32_t four_d,
                               void *host_plan, size_t plan_bytes, tg_packed_info *info);
+/* Plans with an explicit tile schedule (tg_packed_plan(rows_per_warp) is the
+ * schedule {rows_per_warp, 1, 0}). */
+tg_status tg_packed_plan_scheduled(const tg_job *jobs, int32_t n_jobs, const tg_schedule *schedule, int32_t four_d,
+                                   void *plan, size_t plan_bytes, tg_packed_info *info);
+tg_status tg_packed_plan_scheduled_host(const tg_job *jobs, int32_t n_jobs, const tg_schedule *schedule,
+                                        int32_t four_d, void *host_plan, size_t plan_bytes, tg_packed_info *info);
 tg_status tg_packed_projector(const void *plan, const tg_packed_info *info, int32_t mode, int32_t obstacle,
                               void *stream);
 /* Deterministic packed backprojection (TG_BPJ, or TG_BPJT for a 4-D plan):

@@ -172,3 +172,62 @@ def test_deterministic_cg_is_bitwise_isolated():
     ba.copy_(pack.cube_view(b, 3).reshape(-1))
     xa, _ = batch.batched_cg(alone, ba, lam=1e-2, iters=20, graph=False, deterministic=True)
     assert torch.equal(xa, pack.cube_view(x, 3).reshape(-1))
+
+
+# --------------------------------------------------------------------------
+# tile schedules of the autotuner
+
+@pytest.mark.parametrize("sched", [(2, 0, 0), (4, 0, 0), (1, 1, 16), (4, 0, 16)])
+def test_packed_schedules_match_single_job(sched):
+    """Lanes along gamma trace the same rays with the same arithmetic
+    (bitwise-equal projections); 16-step batches regroup the walk's
+    roundings (projection within the image tolerance, backprojection within
+    the cube tolerance).  One job of the pack has views rolled by 90 degrees,
+    the case gamma-major lanes are for."""
+    from helpers import IMG_TOL
+    specs = SPECS[:3]
+    jobs = [synthetic.make_job(s, seed=k) for k, s in enumerate(specs)]
+    ch, vh = synthetic.make_geometry(dict(n=24, T=5, N=48, d=190.0, lon_range=(0.2, 2.5)))
+    for h in vh:
+        h["ROL"] = np.pi / 2
+        for key in [k for k in h if k.startswith("R") and "_" in k]:
+            del h[key]
+    rolled = batch.Job(ch, vh)
+    rolled.phantom = synthetic.phantom(ch, seed=9) / np.float32(1e8)
+    jobs.append(rolled)
+    pack = batch.PackedJobs(jobs, obstacle="sun", schedule=sched)
+    x = pack.new_cube()
+    for k, j in enumerate(jobs):
+        pack.cube_view(x, k).copy_(torch.from_numpy(j.phantom))
+    pack.project(x)
+    rng = np.random.default_rng(6)
+    ys = []
+    for k, j in enumerate(jobs):
+        op = lo_wrapper.siddon_lo(j.view_headers, j.cube_header, obstacle="sun", dtype=np.float32)
+        ref = op.project(torch.from_numpy(j.phantom).cuda())
+        got = pack.data_view(pack.data, k)
+        if sched[2] == 0:
+            torch.testing.assert_close(got, ref, rtol=0, atol=0)
+        else:
+            rel, norm = image_errors(got.cpu().numpy(), ref.cpu().numpy())
+            assert rel <= IMG_TOL and norm <= IMG_TOL, (k, rel, norm)
+        ys.append(rng.random(j.data_shape).astype(np.float32))
+    for k in range(len(jobs)):
+        pack.data_view(pack.data, k).copy_(torch.from_numpy(ys[k]))
+    z = pack.backproject(pack.new_cube())
+    for k, j in enumerate(jobs):
+        op = lo_wrapper.siddon_lo(j.view_headers, j.cube_header, obstacle="sun", dtype=np.float32)
+        ref = op.backproject(torch.from_numpy(ys[k]).cuda())
+        rel, norm = image_errors(pack.cube_view(z, k).cpu().numpy(), ref.cpu().numpy(), sig=CUBE_SIG)
+        assert rel <= CUBE_TOL and norm <= CUBE_TOL, (k, rel, norm)
+
+
+def test_autotune_searches_schedules():
+    jobs, _ = _pack(4)
+    batch.PackedJobs._tune_cache.clear()
+    pack = batch.PackedJobs(jobs, obstacle="sun")
+    table = pack.tune_table
+    assert batch.DEFAULT_SCHEDULE in table and pack.schedule in table
+    assert {(1, 1, 0), (2, 1, 0), (4, 1, 0)} <= set(table)
+    assert any(k[1] == 0 for k in table) and any(k[2] == 16 for k in table)
+    assert table[pack.schedule] == min(table.values())

@@ -25,6 +25,7 @@ UNITS = {
     "reduce.cu": [],
     "noalloc.cu": [],
     "packed.cu": [],
+    "packed_tuned.cu": [],
     "capi.cu": [],
 }
 

@@ -44,7 +44,19 @@ class TgJob(ctypes.Structure):
 class TgPackedInfo(ctypes.Structure):
     _fields_ = [("n_jobs", ctypes.c_int32), ("rows_per_warp", ctypes.c_int32), ("four_d", ctypes.c_int32),
                 ("idx64", ctypes.c_int32), ("tiles", ctypes.c_int64), ("det_workspace_bytes", ctypes.c_int64),
-                ("det_idx64", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("det_idx64", ctypes.c_int32), ("lane_axis", ctypes.c_int32), ("batch_steps", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+class TgSchedule(ctypes.Structure):
+    """Tile schedule of a packed plan: rows per warp (1, 2, 4), the image axis
+    a warp's lanes run along (1: lambda, 0: gamma) and the walk's batch
+    length (0: default, 16)."""
+    _fields_ = [("rows_per_warp", ctypes.c_int32), ("lane_axis", ctypes.c_int32),
+                ("batch_steps", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+DEFAULT_SCHEDULE = (4, 1, 0)
 
 
 def _bind(L):
@@ -57,6 +69,10 @@ def _bind(L):
     L.tg_packed_plan.restype = ctypes.c_int
     L.tg_packed_plan_host.argtypes = [P, I32, I32, I32, P, SZ, P]
     L.tg_packed_plan_host.restype = ctypes.c_int
+    L.tg_packed_plan_scheduled.argtypes = [P, I32, P, I32, P, SZ, P]
+    L.tg_packed_plan_scheduled.restype = ctypes.c_int
+    L.tg_packed_plan_scheduled_host.argtypes = [P, I32, P, I32, P, SZ, P]
+    L.tg_packed_plan_scheduled_host.restype = ctypes.c_int
     L.tg_packed_projector.argtypes = [P, P, I32, I32, P]
     L.tg_packed_projector.restype = ctypes.c_int
     L.tg_packed_backprojector_deterministic.argtypes = [P, P, I32, P, SZ, P]
@@ -111,11 +127,15 @@ class Job:
 
 
 class PackedJobs:
-    """Flat device buffers and packed plans for a list of :class:`Job`s."""
+    """Flat device buffers and packed plans for a list of :class:`Job`s.
+
+    ``schedule`` = (rows per warp, lane axis, batch steps) of the packed
+    tiles (see :class:`TgSchedule`); ``rows_per_warp`` alone means the
+    lambda-major default batches; with neither, :meth:`autotune` picks one."""
 
     _tune_cache = {}
 
-    def __init__(self, jobs, obstacle="sun", rows_per_warp=None, device=None):
+    def __init__(self, jobs, obstacle="sun", rows_per_warp=None, device=None, schedule=None):
         self.L = _bind(_lib.load())
         self.jobs = list(jobs)
         self.n = len(self.jobs)
@@ -136,7 +156,17 @@ class PackedJobs:
         self.data = torch.zeros(int(self.data_off[-1]), dtype=torch.float32, device=dev)
         self._plans = {}
         self._det_ws = None
-        self.rows_per_warp = rows_per_warp or self.autotune()
+        self.tune_table = None
+        if schedule is not None:
+            self.schedule = tuple(int(v) for v in schedule)
+        elif rows_per_warp is not None:
+            self.schedule = (int(rows_per_warp), 1, 0)
+        else:
+            self.schedule = self.autotune()
+
+    @property
+    def rows_per_warp(self):
+        return self.schedule[0]
 
     # views of the flat buffers -------------------------------------------------
     def data_view(self, flat, k):
@@ -158,10 +188,10 @@ class PackedJobs:
         return torch.zeros(int(self.cube_off[-1]), dtype=torch.float32, device=self.device)
 
     # plans ------------------------------------------------------------------------
-    def plan(self, cube_flat, rows_per_warp=None):
+    def plan(self, cube_flat, schedule=None):
         """Device plan tracing all jobs between ``cube_flat`` and ``self.data``."""
-        rpw = rows_per_warp or self.rows_per_warp
-        key = (cube_flat.data_ptr(), rpw)
+        sched = tuple(schedule or self.schedule)
+        key = (cube_flat.data_ptr(), sched)
         if key in self._plans:
             return self._plans[key]
         arr = (TgJob * self.n)()
@@ -186,24 +216,30 @@ class PackedJobs:
         nbytes = self.L.tg_packed_plan_bytes(self.n)
         buf = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
         info = TgPackedInfo()
-        _lib.check(self.L.tg_packed_plan(arr, self.n, rpw, int(self.four_d), _ptr(buf), nbytes, ctypes.byref(info)))
+        sc = TgSchedule(sched[0], sched[1], sched[2], 0)
+        _lib.check(self.L.tg_packed_plan_scheduled(arr, self.n, ctypes.byref(sc), int(self.four_d), _ptr(buf), nbytes,
+                                                   ctypes.byref(info)))
         self._plans[key] = (buf, info, arr)
         return self._plans[key]
 
-    def project(self, cube_flat, rows_per_warp=None):
+    def project(self, cube_flat, schedule=None):
         """self.data = P cube (all jobs, one launch; data zeroed first)."""
-        buf, info, _ = self.plan(cube_flat, rows_per_warp)
+        buf, info, _ = self.plan(cube_flat, schedule)
         self.data.zero_()
         _lib.check(self.L.tg_packed_projector(_ptr(buf), ctypes.byref(info), _lib.TG_PJT if self.four_d else _lib.TG_PJ,
                                               _lib.OBSTACLES[self.obstacle], _stream()))
         return self.data
 
-    def backproject(self, cube_flat, rows_per_warp=None, deterministic=False):
+    def backproject(self, cube_flat, schedule=None, deterministic=False):
         """cube_flat = P^T self.data (all jobs, one launch; cube zeroed first).
         ``deterministic``: every job's cube is bitwise the single-job
         deterministic backprojection of that job alone
-        (``tg_packed_backprojector_deterministic``), whatever the other jobs."""
-        buf, info, _ = self.plan(cube_flat, rows_per_warp)
+        (``tg_packed_backprojector_deterministic``, on lambda-major tiles),
+        whatever the other jobs."""
+        sched = tuple(schedule or self.schedule)
+        if deterministic and sched[1] != 1:
+            sched = (sched[0], 1, sched[2])
+        buf, info, _ = self.plan(cube_flat, sched)
         cube_flat.zero_()
         if deterministic:
             need = int(info.det_workspace_bytes)
@@ -222,27 +258,41 @@ class PackedJobs:
     def signature(self):
         return tuple((j.cube_shape, j.data_shape) for j in self.jobs) + (self.obstacle,)
 
-    def autotune(self, candidates=(1, 2, 4), repeats=2):
-        """Rows per warp (CTA tile height) with the fastest packed pj + bpj."""
+    def _time(self, sched, x, z, repeats):
+        self.project(x, sched)
+        self.backproject(z, sched)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(repeats):
+            self.project(x, sched)
+            self.backproject(z, sched)
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / repeats
+
+    def autotune(self, repeats=2):
+        """Tile schedule with the fastest packed pj + bpj on this job set,
+        by coordinate descent: rows per warp (1, 2, 4) on lambda-major
+        tiles, then the lane axis (lambda / gamma), then the batch length
+        (default / 16).  Cached per job-size signature; the timings are kept
+        in ``tune_table`` ({schedule: seconds per pj + bpj})."""
         sig = self.signature()
         if sig in PackedJobs._tune_cache:
-            return PackedJobs._tune_cache[sig]
+            self.tune_table = PackedJobs._tune_cache[sig][1]
+            return PackedJobs._tune_cache[sig][0]
         x = self.new_cube().fill_(1.0)
         z = self.new_cube()
-        best, best_t = candidates[0], None
-        for rpw in candidates:
-            self.project(x, rpw)
-            self.backproject(z, rpw)
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            for _ in range(repeats):
-                self.project(x, rpw)
-                self.backproject(z, rpw)
-            torch.cuda.synchronize()
-            dt = time.perf_counter() - t0
-            if best_t is None or dt < best_t:
-                best, best_t = rpw, dt
-        PackedJobs._tune_cache[sig] = best
+        table = {}
+
+        def t(sched):
+            if sched not in table:
+                table[sched] = self._time(sched, x, z, repeats)
+            return table[sched]
+        best = min(((rpw, 1, 0) for rpw in (1, 2, 4)), key=t)
+        best = min((best, (best[0], 0, best[2])), key=t)
+        best = min((best, (best[0], best[1], 16)), key=t)
+        self._plans = {k: v for k, v in self._plans.items() if k[0] not in (x.data_ptr(), z.data_ptr())}
+        self.tune_table = table
+        PackedJobs._tune_cache[sig] = (best, table)
         return best
 
 
@@ -269,12 +319,15 @@ def batched_cg(pack, b, lam=1e-2, iters=20, graph=True, deterministic=False):
     hist = torch.zeros(iters + 1, n, dtype=torch.float64, device=dev)
     hist[0] = torch.sqrt(rr / bb)
     k_dev = torch.zeros((), dtype=torch.int64, device=dev)
-    pack.plan(p)
-    pack.plan(Ap)
+    # deterministic mode keeps the default walk batches, so that the
+    # projection is bitwise the single-job one as well
+    sched = (pack.schedule[0], 1, 0) if deterministic else pack.schedule
+    pack.plan(p, sched)
+    pack.plan(Ap, sched)
 
     def step():
-        pack.project(p)
-        pack.backproject(Ap, deterministic=deterministic)
+        pack.project(p, sched)
+        pack.backproject(Ap, sched, deterministic=deterministic)
         if lam:
             ops.axpby(Ap, p, lam, 1.0)          # Ap = lam p + Ap, one fmaf per element
         ops.dot(p, Ap, pAp)

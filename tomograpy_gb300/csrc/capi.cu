@@ -301,35 +301,50 @@ size_t tg_packed_plan_bytes(int32_t n_jobs) {
   return tg::packed_records_offset(n_jobs) + (((size_t)n_jobs * tg::packed_job_bytes() + 255) & ~(size_t)255);
 }
 
-static tg_status build_packed_plan(const tg_job *jobs, int32_t n_jobs, int32_t rows_per_warp, int32_t four_d,
+static tg_status build_packed_plan(const tg_job *jobs, int32_t n_jobs, const tg_schedule &sched, int32_t four_d,
                                    unsigned char *host, tg_packed_info *info);
 
-tg_status tg_packed_plan(const tg_job *jobs, int32_t n_jobs, int32_t rows_per_warp, int32_t four_d, void *plan,
-                         size_t plan_bytes, tg_packed_info *info) {
-  if (!info) return fail(TG_EINVAL, "info is NULL");
+tg_status tg_packed_plan_scheduled(const tg_job *jobs, int32_t n_jobs, const tg_schedule *schedule, int32_t four_d,
+                                   void *plan, size_t plan_bytes, tg_packed_info *info) {
+  if (!info || !schedule) return fail(TG_EINVAL, "info or schedule is NULL");
   if (n_jobs <= 0 || !jobs) return fail(TG_EINVAL, "no jobs");
   if (!plan || plan_bytes < tg_packed_plan_bytes(n_jobs)) return fail(TG_ENOMEM, "plan buffer too small");
   std::vector<unsigned char> host(tg_packed_plan_bytes(n_jobs), 0);
-  tg_status st = build_packed_plan(jobs, n_jobs, rows_per_warp, four_d, host.data(), info);
+  tg_status st = build_packed_plan(jobs, n_jobs, *schedule, four_d, host.data(), info);
   if (st != TG_OK) return st;
   cudaError_t e = cudaMemcpy(plan, host.data(), host.size(), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return launch_status(e, "plan upload");
   return TG_OK;
 }
 
-tg_status tg_packed_plan_host(const tg_job *jobs, int32_t n_jobs, int32_t rows_per_warp, int32_t four_d,
-                              void *host_plan, size_t plan_bytes, tg_packed_info *info) {
-  if (!info) return fail(TG_EINVAL, "info is NULL");
+tg_status tg_packed_plan_scheduled_host(const tg_job *jobs, int32_t n_jobs, const tg_schedule *schedule,
+                                        int32_t four_d, void *host_plan, size_t plan_bytes, tg_packed_info *info) {
+  if (!info || !schedule) return fail(TG_EINVAL, "info or schedule is NULL");
   if (n_jobs <= 0 || !jobs) return fail(TG_EINVAL, "no jobs");
   if (!host_plan || plan_bytes < tg_packed_plan_bytes(n_jobs)) return fail(TG_ENOMEM, "plan buffer too small");
   std::memset(host_plan, 0, tg_packed_plan_bytes(n_jobs));
-  return build_packed_plan(jobs, n_jobs, rows_per_warp, four_d, (unsigned char *)host_plan, info);
+  return build_packed_plan(jobs, n_jobs, *schedule, four_d, (unsigned char *)host_plan, info);
 }
 
-static tg_status build_packed_plan(const tg_job *jobs, int32_t n_jobs, int32_t rows_per_warp, int32_t four_d,
+tg_status tg_packed_plan(const tg_job *jobs, int32_t n_jobs, int32_t rows_per_warp, int32_t four_d, void *plan,
+                         size_t plan_bytes, tg_packed_info *info) {
+  const tg_schedule sched = {rows_per_warp, 1, 0, 0};
+  return tg_packed_plan_scheduled(jobs, n_jobs, &sched, four_d, plan, plan_bytes, info);
+}
+
+tg_status tg_packed_plan_host(const tg_job *jobs, int32_t n_jobs, int32_t rows_per_warp, int32_t four_d,
+                              void *host_plan, size_t plan_bytes, tg_packed_info *info) {
+  const tg_schedule sched = {rows_per_warp, 1, 0, 0};
+  return tg_packed_plan_scheduled_host(jobs, n_jobs, &sched, four_d, host_plan, plan_bytes, info);
+}
+
+static tg_status build_packed_plan(const tg_job *jobs, int32_t n_jobs, const tg_schedule &sched, int32_t four_d,
                                    unsigned char *host, tg_packed_info *info) {
+  const int rows_per_warp = sched.rows_per_warp;
   if (rows_per_warp != 1 && rows_per_warp != 2 && rows_per_warp != 4)
     return fail(TG_EINVAL, "rows_per_warp must be 1, 2 or 4");
+  if (sched.lane_axis != 0 && sched.lane_axis != 1) return fail(TG_EINVAL, "lane_axis must be 0 or 1");
+  if (sched.batch_steps != 0 && sched.batch_steps != 16) return fail(TG_EINVAL, "batch_steps must be 0 or 16");
   const int rows = rows_per_warp * tg::kRows;
   struct Item {
     double work;
@@ -355,6 +370,10 @@ static tg_status build_packed_plan(const tg_job *jobs, int32_t n_jobs, int32_t r
     order[j] = {(double)J.n_views * J.n1 * J.n2 * (double)(J.map_shape[0] + J.map_shape[1] + J.map_shape[2]), j};
   }
   std::stable_sort(order.begin(), order.end(), [](const Item &a, const Item &b) { return a.work > b.work; });
+  // the other schedules are built for 32-bit cube offsets only
+  const bool lmaj = idx64 || sched.lane_axis == 1;
+  const int batch = idx64 ? 0 : sched.batch_steps;
+  const int tile_cols = lmaj ? 32 : rows, tile_rows = lmaj ? rows : 32;
   const size_t rec0 = tg::packed_records_offset(n_jobs);
   long long tiles = 0;
   size_t ws = 0;             // deterministic workspace: one 256-byte aligned part per job
@@ -362,7 +381,7 @@ static tg_status build_packed_plan(const tg_job *jobs, int32_t n_jobs, int32_t r
   for (int k = 0; k < n_jobs; ++k) {
     const int j = order[k].idx;
     const tg_job &J = jobs[j];
-    const int gx = (int)((J.n2 + 31) / 32), gy = (int)((J.n1 + rows - 1) / rows);
+    const int gx = (int)((J.n2 + tile_cols - 1) / tile_cols), gy = (int)((J.n1 + tile_rows - 1) / tile_rows);
     const int64_t shape4[4] = {J.map_shape[0], J.map_shape[1], J.map_shape[2], four_d ? J.map_shape[3] : 1};
     const size_t part = tg_deterministic_workspace_bytes(shape4);
     if (part == SIZE_MAX || ws > SIZE_MAX - part) return fail(TG_EINVAL, "job %d: cube too large", j);
@@ -381,6 +400,8 @@ static tg_status build_packed_plan(const tg_job *jobs, int32_t n_jobs, int32_t r
   info->tiles = tiles;
   info->det_workspace_bytes = (int64_t)ws;
   info->det_idx64 = det_idx64 ? 1 : 0;
+  info->lane_axis = lmaj ? 1 : 0;
+  info->batch_steps = batch;
   info->reserved = 0;
   return TG_OK;
 }
@@ -394,8 +415,10 @@ tg_status tg_packed_projector(const void *plan, const tg_packed_info *info, int3
   if (mode < TG_PJ || mode > TG_BPJT || four_d != (info->four_d != 0))
     return fail(TG_EINVAL, "mode does not match the plan (3-D / 4-D)");
   if (info->tiles <= 0) return TG_OK;
+  if (info->idx64 && (info->lane_axis != 1 || info->batch_steps != 0))
+    return fail(TG_EINVAL, "a plan with 64-bit cube offsets takes the default schedule");
   return launch_status(tg::launch_packed(plan, info->n_jobs, info->tiles, info->rows_per_warp, info->idx64 != 0,
-                                         mode, obstacle, (cudaStream_t)stream),
+                                         mode, obstacle, info->lane_axis, info->batch_steps, (cudaStream_t)stream),
                        "packed projector launch");
 }
 
@@ -406,6 +429,8 @@ tg_status tg_packed_backprojector_deterministic(const void *plan, const tg_packe
     return fail(TG_EINVAL, "obstacle must be none or sun");
   if (info->n_jobs <= 0 || info->n_jobs > 65535) return fail(TG_EINVAL, "plan has %d jobs (1 to 65535)", info->n_jobs);
   if (info->tiles <= 0) return TG_OK;
+  if (info->lane_axis != 1)
+    return fail(TG_EINVAL, "deterministic packed backprojection takes plans with lane_axis 1");
   if (!workspace || ((uintptr_t)workspace & 255u)) return fail(TG_EINVAL, "workspace must be 256-byte aligned");
   if (info->det_workspace_bytes <= 0 || workspace_bytes < (size_t)info->det_workspace_bytes)
     return fail(TG_ENOMEM, "workspace has %zu bytes, the plan needs %lld", workspace_bytes,

@@ -8,61 +8,9 @@
 // finds its job by binary search on the compact tile array, copies the job's
 // record into shared memory and runs the same tile body as the single-job
 // kernel.
-#include "det_common.cuh"
+#include "packed_kernel.cuh"
 
 namespace tg {
-
-struct PackedJob {
-  Geometry G;
-  float *data;
-  float *cube;
-  long long tile0;      // first CTA tile of this job
-  int gx, gy;           // column / row tiles per view
-  // deterministic backprojection: the job's part of the workspace (byte
-  // offset: DetScale, then its int64 accumulator at +256), the accumulator's
-  // dense strides, and the ray count and voxel diagonal behind its scale
-  long long ws_off;
-  long long acc_ms[4];
-  double rays, lmax;
-};
-
-template <int MODE, bool SUN, typename IDX, int RPW, bool DET>
-__global__ void __launch_bounds__(kThreads, min_blocks(MODE))
-    packed_kernel(const long long *__restrict__ tile0, const PackedJob *__restrict__ jobs, int n_jobs,
-                  unsigned char *__restrict__ ws) {
-  static_assert(sizeof(PackedJob) % 4 == 0, "job record copied as 32-bit words");
-  __shared__ int s_job;
-  __shared__ __align__(16) int s_rec[sizeof(PackedJob) / 4];
-  if (threadIdx.x == 0) {
-    const long long b = blockIdx.x;
-    int lo = 0, hi = n_jobs - 1;
-    while (lo < hi) {  // last job whose first tile is <= b
-      const int mid = (lo + hi + 1) >> 1;
-      if (__ldg(tile0 + mid) <= b) lo = mid;
-      else hi = mid - 1;
-    }
-    s_job = lo;
-  }
-  __syncthreads();
-  const int *src = reinterpret_cast<const int *>(jobs + s_job);
-  for (int k = threadIdx.x; k < (int)(sizeof(PackedJob) / 4); k += blockDim.x) s_rec[k] = __ldg(src + k);
-  __syncthreads();
-  PackedJob &J = *reinterpret_cast<PackedJob *>(s_rec);
-  if (DET) {  // the walk indexes the job's dense accumulator instead of its cube
-    if (threadIdx.x < 4) J.G.ms[threadIdx.x] = J.acc_ms[threadIdx.x];
-    __syncthreads();
-  }
-  long long local = (long long)blockIdx.x - J.tile0;
-  const int bx = (int)(local % J.gx);
-  local /= J.gx;
-  const int by = (int)(local % J.gy);
-  const int t = (int)(local / J.gy);
-  constexpr bool PJ = (MODE == TG_PJ || MODE == TG_PJT);
-  unsigned long long *acc = DET ? reinterpret_cast<unsigned long long *>(ws + J.ws_off + 256) : nullptr;
-  const DetScale *dsc = DET ? reinterpret_cast<const DetScale *>(ws + J.ws_off) : nullptr;
-  tile_body<MODE, SUN, IDX, DET, RPW>(J.G, t, bx * 32, by * (RPW * kRows), PJ ? J.cube : J.data,
-                                      PJ ? J.data : J.cube, acc, dsc);
-}
 
 template <int MODE, typename IDX, int RPW, bool DET>
 static void launch_packed_rpw(const long long *tile0, const PackedJob *jobs, int n_jobs, long long tiles, bool sun,
@@ -103,14 +51,15 @@ __global__ void packed_det_finalize(const PackedJob *__restrict__ jobs, unsigned
                      blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
 }
 
-// byte offset of the job records in a plan of n_jobs jobs
-size_t packed_records_offset(int n_jobs) { return ((size_t)n_jobs * sizeof(long long) + 255) & ~(size_t)255; }
+size_t packed_records_offset(int n_jobs) { return packed_records_offset_of(n_jobs); }
 
 cudaError_t launch_packed(const void *plan, int n_jobs, long long tiles, int rpw, bool idx64, int mode, int obstacle,
-                          cudaStream_t s) {
+                          int lane_axis, int batch, cudaStream_t s) {
   const long long *tile0 = (const long long *)plan;
   const PackedJob *jobs = (const PackedJob *)((const unsigned char *)plan + packed_records_offset(n_jobs));
   const bool sun = obstacle == TG_OBSTACLE_SUN;
+  if (lane_axis != 1 || batch != 0)  // the plan builder keeps 64-bit plans on the default schedule
+    return launch_packed_tuned(tile0, jobs, n_jobs, tiles, rpw, mode, sun, lane_axis, batch, s);
   if (idx64) {
     switch (mode) {
     case TG_PJ: launch_packed_mode<TG_PJ, long long>(tile0, jobs, n_jobs, tiles, rpw, sun, s); break;

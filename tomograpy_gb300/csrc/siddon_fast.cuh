@@ -662,16 +662,17 @@ __device__ __forceinline__ void accumulate(float L, IDX o, const float *cin, flo
   }
 }
 
-// Trace ray (i, j) of view t.  See the file header for the arithmetic.
-template <int MODE, bool SUN, typename IDX, bool DET>
+// Trace ray (i, j) of view t; cidx / ridx index its column (lambda) and row
+// (gamma) in the CTA tables.  BATCH: steps per batch (0: the mode's default).
+// See the file header for the arithmetic.
+template <int MODE, bool SUN, typename IDX, bool DET, int BATCH = 0>
 __device__ __forceinline__ void trace_fast(const Geometry &G, const tg_image_header &V, const FastTables &T, int i,
-                                           int j, int t, int row_slot, const float *__restrict__ xin,
+                                           int j, int t, int cidx, int ridx, const float *__restrict__ xin,
                                            float *__restrict__ xout, unsigned long long *__restrict__ acc64,
                                            const DetScale *__restrict__ dsc) {
   constexpr bool CNT = (MODE == kModeCount);
   constexpr bool PJ = (MODE == TG_PJ || MODE == TG_PJT || CNT);
   constexpr bool T4 = (MODE == TG_PJT || MODE == TG_BPJT);
-  const int lane = threadIdx.x & 31;
   if (i >= G.n1 || j >= G.n2) return;
   if (G.ray_i >= 0 && (i != G.ray_i || j != G.ray_j)) return;
   if (masked(G, i, j, t)) return;
@@ -689,7 +690,7 @@ __device__ __forceinline__ void trace_fast(const Geometry &G, const tg_image_hea
   }
   Walk<IDX> w;
   float sun_lo;
-  if (!setup_ray<SUN, IDX>(G, V, T, lane, row_slot, w, sun_lo)) return;
+  if (!setup_ray<SUN, IDX>(G, V, T, cidx, ridx, w, sun_lo)) return;
   yv *= w.lscale;  // lengths of the walk parameter -> path lengths
 
   const float *cin = PJ ? xin + fbase : nullptr;
@@ -726,7 +727,7 @@ __device__ __forceinline__ void trace_fast(const Geometry &G, const tg_image_hea
   // (kBatch + 3) 2^-23 h, so a drifted step still advances only families
   // whose exact crossing is below the stop.  The counts are then recovered
   // (resync) and the batch's last step is an exact one.
-  constexpr int kBatch = batch_steps(MODE);
+  constexpr int kBatch = BATCH ? BATCH : batch_steps(MODE);
   constexpr bool kDrift = drift_batches(MODE);
   const float margin = kDrift ? (float)(kBatch + 3) * 1.1920929e-7f * (-w.t0) : 0.f;
   while (guard >= kBatch) {
@@ -853,7 +854,7 @@ __device__ __forceinline__ void trace_fast(const Geometry &G, const tg_image_hea
         int ivn[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) ivn[k] = w.iv0[k] + w.upd[k] * (int)w.m[k];
-        outside = exact_outside(G, V, T, lane, row_slot, ivn);
+        outside = exact_outside(G, V, T, cidx, ridx, ivn);
       }
       if (!outside) break;
       IDX o;
@@ -866,14 +867,20 @@ __device__ __forceinline__ void trace_fast(const Geometry &G, const tg_image_hea
   if (CNT && acc != 0.f) xout[po] += acc;
 }
 
-// One CTA tile: rows [row0, row0 + 8 * RPW) x columns [col0, col0 + 32) of
-// view t; warp w traces rows w, w + 8, ... of the tile (RPW rows per warp).
-template <int MODE, bool SUN, typename IDX, bool DET, int RPW>
+// One CTA tile of view t.  LMAJ (lanes along lambda, image axis 1): rows
+// [row0, row0 + 8 * RPW) x columns [col0, col0 + 32), warp w traces rows
+// w, w + 8, ... (RPW rows per warp), its lanes 32 neighbouring columns.
+// Otherwise lanes run along gamma (image axis 0): rows [row0, row0 + 32) x
+// columns [col0, col0 + 8 * RPW), warp w traces columns w, w + 8, ... --
+// the better mapping when image axis 0 follows the cube's fastest axis (a
+// view rolled by 90 degrees).  The CTA tables cover 32 rows and 32 columns
+// either way.
+template <int MODE, bool SUN, typename IDX, bool DET, int RPW, bool LMAJ = true, int BATCH = 0>
 __device__ __forceinline__ void tile_body(const Geometry &G, int t, int col0, int row0,
                                           const float *__restrict__ xin, float *__restrict__ xout,
                                           unsigned long long *__restrict__ acc64,
                                           const DetScale *__restrict__ dsc) {
-  static_assert(RPW * kRows <= kFastRows, "tile taller than the CTA tables");
+  static_assert(RPW * kRows <= kFastRows && kFastRows == 32, "tile larger than the CTA tables");
   __shared__ FastTables T;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const tg_image_header &V = G.views[t];
@@ -882,7 +889,12 @@ __device__ __forceinline__ void tile_body(const Geometry &G, int t, int col0, in
 #pragma unroll 1
   for (int r = 0; r < RPW; ++r) {
     const int slot = warp + r * kRows;
-    trace_fast<MODE, SUN, IDX, DET>(G, V, T, row0 + slot, col0 + lane, t, slot, xin, xout, acc64, dsc);
+    if (LMAJ)
+      trace_fast<MODE, SUN, IDX, DET, BATCH>(G, V, T, row0 + slot, col0 + lane, t, lane, slot, xin, xout, acc64,
+                                             dsc);
+    else
+      trace_fast<MODE, SUN, IDX, DET, BATCH>(G, V, T, row0 + lane, col0 + slot, t, slot, lane, xin, xout, acc64,
+                                             dsc);
   }
 }
 

@@ -77,7 +77,10 @@ cudaError_t launch_deterministic_bpj(const Geometry &G, int mode, int obstacle, 
                                      cudaStream_t s);
 
 cudaError_t launch_packed(const void *plan, int n_jobs, long long tiles, int rpw, bool idx64, int mode, int obstacle,
-                          cudaStream_t s);
+                          int lane_axis, int batch, cudaStream_t s);
+struct PackedJob;
+cudaError_t launch_packed_tuned(const long long *tile0, const PackedJob *jobs, int n_jobs, long long tiles, int rpw,
+                                int mode, bool sun, int lane_axis, int batch, cudaStream_t s);
 size_t packed_job_bytes();
 size_t packed_records_offset(int n_jobs);
 void packed_fill(void *dst, const Geometry &G, float *data, float *cube, long long tile0, int gx, int gy,

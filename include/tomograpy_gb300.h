@@ -52,6 +52,12 @@ typedef enum {
 } tg_status;
 
 typedef enum { TG_PJ = 0, TG_BPJ = 1, TG_PJT = 2, TG_BPJT = 3 } tg_mode;
+/* Flag ORed into TG_PJ / TG_PJT (f32 data) of the projector entry points:
+ * every pixel of the traced views is written -- the projection, or 0 where
+ * the ray is masked or misses the cube -- instead of added, so the stack
+ * needs no zeroing first (e.g. a stack in page-locked host memory written
+ * directly by the kernel, see tg_host_alias).  The reference always adds. */
+#define TG_OVERWRITE 16
 typedef enum { TG_OBSTACLE_NONE = 0, TG_OBSTACLE_SUN = 1 } tg_obstacle;
 typedef enum { TG_F32 = 0, TG_F64 = 1, TG_U8 = 2 } tg_dtype;
 
@@ -289,6 +295,13 @@ tg_status tg_cg_update_p(float *p, const float *r, double *rr, const double *rr_
  * beta = 0, y = alpha x -- e.g. clearing a job's vectors or adding lam x). */
 tg_status tg_segmented_axpby(float *y, const float *x, float alpha, float beta, const int64_t *seg, int32_t n_seg,
                              void *stream);
+
+/* Device address of page-locked host memory (e.g. cudaHostAlloc'd, or a
+ * pinned torch tensor) that the GPU can read and write directly over the
+ * host link: a data stack there can be passed to the projectors without a
+ * staging copy.  TG_EINVAL when the pointer is not such memory.  No
+ * counterpart in the reference. */
+tg_status tg_host_alias(const void *host, void **device);
 
 /* Message for the last non-OK status returned on this thread. */
 const char *tg_last_error(void);

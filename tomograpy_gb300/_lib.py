@@ -10,6 +10,7 @@ from . import _build
 
 TG_OK, TG_EINVAL, TG_ENOMEM, TG_ELAUNCH, TG_EUNSUPPORTED = 0, 1, 2, 3, 4
 TG_PJ, TG_BPJ, TG_PJT, TG_BPJT = 0, 1, 2, 3
+TG_OVERWRITE = 16
 TG_OBSTACLE_NONE, TG_OBSTACLE_SUN = 0, 1
 TG_F32, TG_F64, TG_U8 = 0, 1, 2
 
@@ -72,6 +73,8 @@ def load(build_if_missing=True):
     for name in ("tg_dot_f32", "tg_segment_counts", "tg_conic_full_projector", "tg_conic_image_projector", "tg_ray_projector", "tg_unit_vector",
                  "tg_intersection_parameters", "tg_conic_full_backprojector_deterministic"):
         getattr(L, name).restype = ctypes.c_int
+    L.tg_host_alias.argtypes = [P, ctypes.POINTER(P)]
+    L.tg_host_alias.restype = ctypes.c_int
     L.tg_last_error.restype = ctypes.c_char_p
     L.tg_last_error.argtypes = []
     L.tg_abi_version.restype = ctypes.c_int32
@@ -91,3 +94,15 @@ def check(status):
 def i64(values):
     vals = list(values)
     return (ctypes.c_int64 * len(vals))(*vals)
+
+
+def host_alias(t):
+    """Device address of a pinned (page-locked) host tensor that kernels can
+    read and write directly over the host link, or None when ``t`` is not
+    such memory (pageable host memory, device memory)."""
+    if t is None or t.is_cuda or not t.is_pinned():
+        return None
+    out = ctypes.c_void_p()
+    if load().tg_host_alias(ctypes.c_void_p(t.data_ptr()), ctypes.byref(out)) != TG_OK:
+        return None
+    return out.value

@@ -93,7 +93,11 @@ tg_status project_views(const tg_map_header *mh, const tg_image_header *views, i
                         const int64_t ds[3], void *map, const int64_t map_shape[4], const int64_t ms[4],
                         const void *mask, tg_dtype mask_dtype, const int64_t ks[3], int32_t obstacle,
                         int32_t mode, void *stream) {
+  const bool overwrite = (mode & TG_OVERWRITE) != 0;
+  mode &= ~TG_OVERWRITE;
   if (mode < TG_PJ || mode > TG_BPJT) return fail(TG_EINVAL, "mode must be pj, bpj, pjt or bpjt");
+  if (overwrite && (mode == TG_BPJ || mode == TG_BPJT)) return fail(TG_EINVAL, "overwrite is for projections");
+  if (overwrite && dtype != TG_F32) return fail(TG_EUNSUPPORTED, "overwrite projections take f32 data");
   if (obstacle != TG_OBSTACLE_NONE && obstacle != TG_OBSTACLE_SUN)
     return fail(TG_EINVAL, "obstacle must be none or sun");
   if (dtype != TG_F32 && dtype != TG_F64) return fail(TG_EINVAL, "data dtype must be f32 or f64");
@@ -109,6 +113,7 @@ tg_status project_views(const tg_map_header *mh, const tg_image_header *views, i
   cudaStream_t s = (cudaStream_t)stream;
   int gx, gy;
   const int rows = (dtype == TG_F32) ? tg::kFastRows : tg::kRows;
+  G.overwrite = overwrite ? 1 : 0;
   if (ray_i >= 0) {
     G.ray_i = ray_i;
     G.ray_j = ray_j;
@@ -509,6 +514,21 @@ tg_status tg_dot_f32(const float *a, const float *b, int64_t n, double *out, voi
   if (!workspace || workspace_bytes < tg_dot_workspace_bytes() || ((uintptr_t)workspace & 7u))
     return fail(TG_ENOMEM, "dot workspace needs %zu bytes, 8-byte aligned", tg_dot_workspace_bytes());
   return launch_status(tg::launch_dot(a, b, n, (double *)workspace, out, (cudaStream_t)stream), "dot launch");
+}
+
+tg_status tg_host_alias(const void *host, void **device) {
+  if (!host || !device) return fail(TG_EINVAL, "NULL argument");
+  *device = nullptr;
+  cudaPointerAttributes a;
+  cudaError_t e = cudaPointerGetAttributes(&a, host);
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // clear the sticky-free error of an unknown pointer
+    return launch_status(e, "pointer attributes");
+  }
+  if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr)
+    return fail(TG_EINVAL, "not page-locked host memory mapped into the device's address space");
+  *device = a.devicePointer;
+  return TG_OK;
 }
 
 const char *tg_last_error(void) { return g_err; }

@@ -675,14 +675,23 @@ __device__ __forceinline__ void trace_fast(const Geometry &G, const tg_image_hea
   constexpr bool T4 = (MODE == TG_PJT || MODE == TG_BPJT);
   if (i >= G.n1 || j >= G.n2) return;
   if (G.ray_i >= 0 && (i != G.ray_i || j != G.ray_j)) return;
-  if (masked(G, i, j, t)) return;
+  const long long po = (long long)i * G.ds[0] + (long long)j * G.ds[1] + (long long)t * G.ds[2];
+  // overwrite mode (projection): every pixel is written, 0 where the ray is
+  // skipped, so the stack needs no zeroing pass first
+  const bool ovw = PJ && !CNT && G.overwrite;
+  if (masked(G, i, j, t)) {
+    if (ovw) xout[po] = 0.f;
+    return;
+  }
   long long fbase = 0;
   if (T4) {
     const int f = V.frame;
-    if (f < 0 || f >= G.nframes) return;
+    if (f < 0 || f >= G.nframes) {
+      if (ovw) xout[po] = 0.f;
+      return;
+    }
     fbase = (long long)f * G.ms[3];
   }
-  const long long po = (long long)i * G.ds[0] + (long long)j * G.ds[1] + (long long)t * G.ds[2];
   float yv = 0.f;
   if (!PJ) {
     yv = xin[po];
@@ -690,7 +699,10 @@ __device__ __forceinline__ void trace_fast(const Geometry &G, const tg_image_hea
   }
   Walk<IDX> w;
   float sun_lo;
-  if (!setup_ray<SUN, IDX>(G, V, T, cidx, ridx, w, sun_lo)) return;
+  if (!setup_ray<SUN, IDX>(G, V, T, cidx, ridx, w, sun_lo)) {
+    if (ovw) xout[po] = 0.f;
+    return;
+  }
   yv *= w.lscale;  // lengths of the walk parameter -> path lengths
 
   const float *cin = PJ ? xin + fbase : nullptr;
@@ -863,7 +875,8 @@ __device__ __forceinline__ void trace_fast(const Geometry &G, const tg_image_hea
     }
   }
   acc += part;
-  if (PJ && !CNT && acc != 0.f) xout[po] += acc * w.lscale;
+  if (ovw) xout[po] = acc * w.lscale;
+  else if (PJ && !CNT && acc != 0.f) xout[po] += acc * w.lscale;
   if (CNT && acc != 0.f) xout[po] += acc;
 }
 

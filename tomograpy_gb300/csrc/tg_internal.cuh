@@ -41,6 +41,7 @@ struct Geometry {
   long long ks[3];
   int mask_dtype;      // tg_dtype
   int mask_eq1;        // 1: skip when mask == 1 (ray_projector); 0: skip when mask != 0
+  int overwrite;       // projection: write every traced pixel (0 where skipped) instead of adding
   int n[3];            // cube voxels per axis
   int nframes;         // frames of a 4-D cube (1 for 3-D)
   long long ms[4];     // cube strides (elements)

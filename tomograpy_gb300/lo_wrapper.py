@@ -24,6 +24,7 @@ Differences from the reference, on purpose:
 """
 import numpy as np
 
+from . import _lib
 from . import siddon as S
 
 try:
@@ -118,6 +119,35 @@ class Siddon(LinearOperator):
         return (torch.is_tensor(host) and not host.is_cuda and host.is_pinned() and self.n1 >= 64
                 and self.tdtype == torch.float32 and host.dtype == torch.float32)
 
+    # pinned host stacks: traced in place over the host link when the GPU can
+    # address them (True), else staged in row blocks
+    HOST_DIRECT = True
+
+    def _host_stack(self, host):
+        """(stack view, device alias) of a pinned float32 host stack the kernels
+        can read / write in place over the host link, or None.  Taken when the
+        stack's image axis 1 is contiguous (e.g. view-major (T, N1, N2)
+        storage presented as (N1, N2, T))."""
+        if not (self.HOST_DIRECT and torch.is_tensor(host) and not host.is_cuda and host.is_pinned()
+                and host.dtype == torch.float32 and self.tdtype == torch.float32):
+            return None
+        stack = host if tuple(host.shape) == self.data_shape else None
+        if stack is None:
+            if not host.is_contiguous() or host.numel() != int(np.prod(self.data_shape)):
+                return None
+            stack = host.view(self.data_shape)
+        if stack.stride(1) != 1:
+            # a warp's lanes hold neighbouring pixels along image axis 1: with
+            # that axis strided (e.g. the reference's (N1, N2, T) order, T
+            # fastest) the lanes' host accesses do not coalesce and the link
+            # carries a transaction per pixel (measured 2x slower than the
+            # row-block staging), so such stacks are staged
+            return None
+        alias = _lib.host_alias(host)
+        if alias is None:
+            return None
+        return stack, alias + (stack.data_ptr() - host.data_ptr())
+
     def _copy_stream(self):
         if self._stream is None:
             self._stream = torch.cuda.Stream(device=self.device)
@@ -160,9 +190,21 @@ class Siddon(LinearOperator):
 
     def project(self, x, out=None):
         """y = P x.  ``x``: cube (CUDA or host tensor / array).  Returns a CUDA
-        tensor, or fills ``out`` (device or host tensor) and returns it; a
-        pinned host ``out`` is filled block by block while the GPU traces."""
+        tensor, or fills ``out`` (device or host tensor) and returns it.  A
+        pinned float32 host ``out`` whose image axis 1 is contiguous is written
+        by the kernel itself over the host link -- every pixel, so it needs no
+        zeroing and no staging copy; other pinned stacks are filled block by
+        block while the GPU traces."""
         xd = self._dev(x, self.cube_shape)
+        hs = self._host_stack(out) if out is not None else None
+        if hs is not None:
+            # the kernel writes every pixel of the pinned host stack directly
+            # (overwrite mode: no zeroing pass, no staging copy)
+            stack, alias = hs
+            S.run_device("pjt" if self.four_d else "pj", stack, xd, self.views_dev, self.mh, self.n_views, self.mask,
+                         self.obstacle, overwrite=True, data_ptr=alias)
+            torch.cuda.current_stream().synchronize()
+            return out
         if out is not None and self._pipelined(out):
             return self._project_to_host(xd, out)
         y = torch.zeros(self.data_shape, dtype=self.tdtype, device=self.device)
@@ -171,23 +213,31 @@ class Siddon(LinearOperator):
         return self._out(y, out)
 
     def backproject(self, y, out=None):
-        """x = P^T y.  ``y``: data stack (CUDA or host tensor / array; a pinned
-        host stack is sent block by block while the GPU traces)."""
-        if self._pipelined(y) and not self.deterministic:
+        """x = P^T y.  ``y``: data stack (CUDA or host tensor / array).  A
+        pinned float32 host stack whose image axis 1 is contiguous is read by
+        the kernel itself over the host link; other pinned stacks are sent
+        block by block while the GPU traces."""
+        hs = self._host_stack(y)
+        if hs is not None:
+            # the kernel reads the pinned host stack directly
+            yd, alias = hs
+        elif self._pipelined(y) and not self.deterministic:
             return self._backproject_from_host(y, out)
-        yd = self._dev(y, self.data_shape)
+        else:
+            yd, alias = self._dev(y, self.data_shape), None
         x = self.new_cube()
         if self.deterministic and self.tdtype == torch.float32:
-            from . import _lib
             need = _lib.load().tg_deterministic_workspace_bytes(
                 _lib.i64(list(self.cube_shape) + ([] if self.four_d else [1])))
             if self._workspace is None or self._workspace.numel() < need:
                 self._workspace = torch.empty(need, dtype=torch.uint8, device=self.device)
             S.run_device("bpjt" if self.four_d else "bpj", yd, x, self.views_dev, self.mh, self.n_views, self.mask,
-                         self.obstacle, deterministic=True, workspace=self._workspace)
+                         self.obstacle, deterministic=True, workspace=self._workspace, data_ptr=alias)
         else:
             S.run_device("bpjt" if self.four_d else "bpj", yd, x, self.views_dev, self.mh, self.n_views, self.mask,
-                         self.obstacle)
+                         self.obstacle, data_ptr=alias)
+        if alias is not None and out is None:
+            torch.cuda.current_stream().synchronize()   # the caller may reuse its host stack at once
         return self._out(x, out)
 
     def _out(self, r, out):

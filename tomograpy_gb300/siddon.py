@@ -146,20 +146,23 @@ def _dtype_code(t):
 # device-level core (torch tensors on the GPU)
 
 def run_device(mode, data, cube, views_dev, map_header, n_views, mask=None, obstacle=None, view=None,
-               ray=None, deterministic=False, workspace=None):
+               ray=None, deterministic=False, workspace=None, overwrite=False, data_ptr=None):
     """Launch one projector call on CUDA tensors (in place, on the current stream).
 
     data: (N1, N2, T) tensor; cube: (n0, n1, n2) or (n0, n1, n2, F) tensor;
     views_dev: uint8 device tensor from :func:`upload_views`; map_header: a
-    dict or a packed ``MapHeader``.
+    dict or a packed ``MapHeader``.  ``overwrite`` (projections): every pixel
+    is written instead of added.  ``data_ptr``: the device address to use for
+    ``data`` -- a pinned host tensor's :func:`_lib.host_alias`, so that the
+    kernel reads / writes the stack in host memory directly.
     """
     L = _lib.load()
     mode_i = _lib.MODES[mode] if isinstance(mode, str) else int(mode)
     if obstacle not in _lib.OBSTACLES:
         raise ValueError("obstacle must be None or 'sun'")
     obst = _lib.OBSTACLES[obstacle]
-    if not (data.is_cuda and cube.is_cuda):
-        raise ValueError("data and cube must be CUDA tensors")
+    if not (cube.is_cuda and (data.is_cuda or data_ptr is not None)):
+        raise ValueError("data and cube must be CUDA tensors (or data a pinned host tensor with its alias)")
     if data.dtype != cube.dtype:
         raise ValueError("data and cube map should have the same data-type")
     dt = _dtype_code(data)
@@ -184,17 +187,21 @@ def run_device(mode, data, cube, views_dev, map_header, n_views, mask=None, obst
     else:
         mptr, mdt, mstr = None, _lib.TG_U8, _lib.i64([0, 0, 0])
     n1, n2 = int(data.shape[0]), int(data.shape[1])
-    common = (dt, ctypes.c_void_p(data.data_ptr()), n1, n2, _strides(data), ctypes.c_void_p(cube.data_ptr()),
-              _lib.i64(cshape), _lib.i64(cstr), mptr, mdt, mstr, obst, mode_i, _stream_ptr())
+    dptr = data.data_ptr() if data_ptr is None else int(data_ptr)
+    if overwrite and mode_i not in (_lib.TG_PJ, _lib.TG_PJT):
+        raise ValueError("overwrite is for projections")
+    common = (dt, ctypes.c_void_p(dptr), n1, n2, _strides(data), ctypes.c_void_p(cube.data_ptr()),
+              _lib.i64(cshape), _lib.i64(cstr), mptr, mdt, mstr, obst,
+              mode_i | (_lib.TG_OVERWRITE if overwrite else 0), _stream_ptr())
     vptr = ctypes.c_void_p(views_dev.data_ptr())
     if deterministic:
         if dt != _lib.TG_F32 or mode_i not in (_lib.TG_BPJ, _lib.TG_BPJT) or view is not None or ray is not None:
             raise ValueError("deterministic mode is for float32 full backprojection")
         need = L.tg_deterministic_workspace_bytes(_lib.i64(cshape if four_d else cshape[:3] + [1]))
         if workspace is None or workspace.numel() * workspace.element_size() < need:
-            workspace = torch.empty(need, dtype=torch.uint8, device=data.device)
+            workspace = torch.empty(need, dtype=torch.uint8, device=cube.device)
         st = L.tg_conic_full_backprojector_deterministic(
-            ctypes.byref(mh), vptr, n_views, ctypes.c_void_p(data.data_ptr()), n1, n2, _strides(data),
+            ctypes.byref(mh), vptr, n_views, ctypes.c_void_p(dptr), n1, n2, _strides(data),
             ctypes.c_void_p(cube.data_ptr()), _lib.i64(cshape), _lib.i64(cstr), mptr, mdt, mstr, obst, mode_i,
             ctypes.c_void_p(workspace.data_ptr()), workspace.numel() * workspace.element_size(), _stream_ptr())
     elif ray is not None:

@@ -25,8 +25,17 @@ struct PackedJob {
 // LMAJ / BATCH: the tile schedule (lanes along lambda or gamma, steps per
 // batch; see tile_body); the plan's tile counts gx, gy follow the same
 // schedule.
+#ifndef TG_PACKED_PJ_MIN_BLOCKS
+#define TG_PACKED_PJ_MIN_BLOCKS TG_PJ_MIN_BLOCKS
+#endif
+// CTAs per SM the packed kernel's register budget allows (its job record and
+// schedule state make it heavier than the single-job kernel)
+__host__ __device__ constexpr int packed_min_blocks(int mode) {
+  return is_backprojection(mode) ? TG_BPJ_MIN_BLOCKS : TG_PACKED_PJ_MIN_BLOCKS;
+}
+
 template <int MODE, bool SUN, typename IDX, int RPW, bool DET, bool LMAJ = true, int BATCH = 0>
-__global__ void __launch_bounds__(kThreads, min_blocks(MODE))
+__global__ void __launch_bounds__(kThreads, packed_min_blocks(MODE))
     packed_kernel(const long long *__restrict__ tile0, const PackedJob *__restrict__ jobs, int n_jobs,
                   unsigned char *__restrict__ ws) {
   static_assert(sizeof(PackedJob) % 4 == 0, "job record copied as 32-bit words");

@@ -3,8 +3,8 @@
 * recon256: the 256^3 cube with the shell + blob phantom and 512 x 512 views
   of the 360-view circle at d = 215 (five of its views, spread over 0-360 deg,
   plus views at exactly lon = pi/2 and pi, whose central rows are degenerate
-  and excluded as everywhere else): 214 voxel segments per ray on average,
-  four times the chord of the 64^3 case;
+  and excluded as everywhere else; and the whole 360-view orbit): 214 voxel
+  segments per ray on average, four times the chord of the 64^3 case;
 * frames128: the 128^3 x 28-frame time-dependent geometry with 784 views of
   256 x 256 (view v in frame v // 28): the views of three frames, with their
   real frame numbers, traced into / out of a 28-frame cube;
@@ -100,6 +100,37 @@ def test_recon256_views_against_oracle():
     record("recon256_bpj", rel=rel, norm=norm, views=T, worst_voxel=[int(v) for v in worst],
            worst_value_frac=float(cref[worst] / np.abs(cref).max()),
            worst_abs_err=float(abs(c[worst] - cref[worst])))
+    assert rel <= CUBE_TOL and norm <= CUBE_TOL, (rel, norm)
+
+
+def test_recon256_full_orbit_against_oracle():
+    """The benchmark's own configuration, every one of its 360 views: the
+    phantom's projection and the backprojection of a random stack against the
+    float64 oracle (~25 s of oracle time on 16 host cores)."""
+    cfg = synthetic.CONFIGS["recon256"]
+    n, N, T = cfg["n"], cfg["N"], cfg["T"]
+    ch, vh = synthetic.make_geometry("recon256")
+    degen = degenerate_rays(vh, N, N)
+    x = synthetic.phantom(ch, seed=0)
+    dev = torch.device("cuda")
+    views = tg.siddon.upload_views(vh, None, dev)
+    mh = tg.siddon.pack_map_header(ch)
+    y = torch.zeros((T, N, N), device=dev).permute(1, 2, 0)
+    tg.siddon.run_device("pj", y, torch.from_numpy(x).to(dev), views, mh, T, obstacle="sun")
+    y = y.cpu().numpy()
+    ref = _oracle_pj(vh, ch, x, N, N)
+    rel, norm = image_errors(y, ref, exclude=degen)
+    record("recon256_full_pj", rel=rel, norm=norm, views=T, worst=worst_element(y, ref, degen))
+    assert rel <= IMG_TOL and norm <= IMG_TOL, (rel, norm)
+    del ref
+    yy = np.random.default_rng(14).random((N, N, T)).astype(np.float32)
+    yy[degen] = 0
+    c = torch.zeros((n, n, n), device=dev)
+    yt = torch.from_numpy(np.ascontiguousarray(yy.transpose(2, 0, 1))).to(dev).permute(1, 2, 0)
+    tg.siddon.run_device("bpj", yt, c, views, mh, T, obstacle="sun")
+    cref = _oracle_bpj(vh, ch, yy, (n, n, n))
+    rel, norm = image_errors(c.cpu().numpy(), cref, sig=CUBE_SIG)
+    record("recon256_full_bpj", rel=rel, norm=norm, views=T)
     assert rel <= CUBE_TOL and norm <= CUBE_TOL, (rel, norm)
 
 

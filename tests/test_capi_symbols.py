@@ -112,3 +112,66 @@ def test_deterministic_entry_points_reject_overflowing_cubes(lib):
     st = lib.tg_conic_full_projector(ctypes.byref(mh), buf, 1, 0, buf, 1, 1, _lib.i64([1, 1, 1]), buf, shape4,
                                      _lib.i64([64, 8, 1, 512]), None, 2, _lib.i64([0, 0, 0]), 0, _lib.TG_PJT, None)
     assert st == _lib.TG_EINVAL and b"frames" in lib.tg_last_error()
+
+
+def _host_job(n=16, N=32, T=4):
+    """A tg_job whose pointers are never dereferenced by the host-side plan."""
+    from tomograpy_gb300 import batch
+    J = batch.TgJob()
+    for k in range(3):
+        J.map_header.cdelt[k] = 3.0 / n
+        J.map_header.pshape[k] = 3.0
+        J.map_header.mmin[k] = -1.5
+        J.map_header.mmax[k] = 1.5
+        J.map_shape[k] = n
+    J.map_shape[3] = 1
+    J.map_strides[0], J.map_strides[1], J.map_strides[2] = n * n, n, 1
+    J.views = 1 << 20                      # placeholders: a host plan only records them
+    J.n_views = T
+    J.n1 = J.n2 = N
+    J.data_strides[0], J.data_strides[1], J.data_strides[2] = N, 1, N * N
+    J.mask_dtype = _lib.TG_U8
+    J.data = 1 << 21
+    J.map = 1 << 22
+    return J
+
+
+def test_host_plan_schedules_and_workspace(lib):
+    """tg_packed_plan_scheduled_host: tile counts follow the schedule, the
+    deterministic workspace covers every job, bad schedules are rejected --
+    all on the host."""
+    from tomograpy_gb300 import batch
+    batch._bind(lib)
+    jobs = (batch.TgJob * 2)(_host_job(16, 32, 4), _host_job(24, 64, 3))
+    nbytes = lib.tg_packed_plan_bytes(2)
+    buf = ctypes.create_string_buffer(nbytes)
+    tiles = {}
+    for sched in ((4, 1, 0), (1, 1, 16), (2, 0, 0)):
+        info = batch.TgPackedInfo()
+        sc = batch.TgSchedule(*sched, 0)
+        st = lib.tg_packed_plan_scheduled_host(jobs, 2, ctypes.byref(sc), 0, buf, nbytes, ctypes.byref(info))
+        assert st == _lib.TG_OK, lib.tg_last_error()
+        assert (info.rows_per_warp, info.lane_axis, info.batch_steps) == sched
+        rows = 8 * sched[0]
+        tc, tr = (32, rows) if sched[1] else (rows, 32)
+        want = sum(-(-N // tc) * -(-N // tr) * T for (N, T) in ((32, 4), (64, 3)))
+        assert info.tiles == want
+        ws = lib.tg_deterministic_workspace_bytes(_lib.i64([16, 16, 16, 1])) + \
+            lib.tg_deterministic_workspace_bytes(_lib.i64([24, 24, 24, 1]))
+        assert info.det_workspace_bytes == ws
+        tiles[sched] = info.tiles
+    for bad in ((3, 1, 0), (4, 2, 0), (4, 1, 8)):
+        info = batch.TgPackedInfo()
+        st = lib.tg_packed_plan_scheduled_host(jobs, 2, ctypes.byref(batch.TgSchedule(*bad, 0)), 0, buf, nbytes,
+                                               ctypes.byref(info))
+        assert st == _lib.TG_EINVAL
+
+
+def test_host_alias_rejects_plain_memory(lib):
+    """Pageable host memory has no device alias (and without a GPU the query
+    itself fails cleanly)."""
+    buf = ctypes.create_string_buffer(64)
+    out = ctypes.c_void_p()
+    assert lib.tg_host_alias(buf, ctypes.byref(out)) != _lib.TG_OK
+    assert out.value is None
+    assert lib.tg_host_alias(None, ctypes.byref(out)) == _lib.TG_EINVAL

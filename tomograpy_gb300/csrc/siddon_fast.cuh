@@ -5,7 +5,8 @@
 // i.e. 32 rays that are neighbours along image axis 1 (lambda).  For observers near the
 // solar equator that axis maps to the cube's fastest axis, so at a given step
 // the warp's lanes read / update neighbouring voxels of one cube row and the
-// whole warp walks the same (x, y) voxel sequence in lock step.
+// whole warp walks the same (x, y) voxel sequence in lock step.  (The packed
+// kernel can also run lanes along image axis 0, see tile_body.)
 //
 // Arithmetic (the reference does everything in its C type,
 // tomograpy/C_siddon.c.template:530-580,811-912):
@@ -13,8 +14,11 @@
 //    products) from per-CTA tables computed in double precision: direction
 //    cos l * (A_row + tan l * R[:, 2]) with A_row = R . (cos g, sin g, 0),
 //    entry parameter, entry point (the two ~d-sized terms cancel to ~1e-11),
-//    entry voxel by a floor division against the exact plane positions, and
-//    the crossing spacing CDELT / |w|.  Single precision only classifies the
+//    entry voxel by a floor division against the exact plane positions, the
+//    remainder and the first crossing of each family (a float remainder
+//    divided by a small |w| would misplace a nearly parallel family's
+//    crossings), and the crossing spacing CDELT / |w|.  Single precision only
+//    classifies the
 //    ray (miss / clear entry face); the full double-precision reference
 //    set-up (siddon_geom.cuh) runs when that classification is within its
 //    error bound;
@@ -27,7 +31,8 @@
 //    never occurs.  Steps run in batches that are proven, by one bound, to
 //    start before the stop parameter, so a batch needs no per-step test and
 //    its gathers / atomics are issued together; inside a batch the crossings
-//    advance by running sums (one add) and are recomputed exactly after it;
+//    advance by running sums (one add) in a frame local to the batch and are
+//    recomputed exactly after it;
 //  * the "sun" obstacle: the reference tests |M + ac u|^2 > 1 at every voxel
 //    entry (:575).  Here the walk runs unchecked up to the sphere-entry
 //    parameter minus an error bound; from there on every voxel entry is tested

@@ -27,7 +27,8 @@ import pytest
 
 import oracle
 import tomograpy_gb300 as tg
-from helpers import CUBE_SIG, CUBE_TOL, IMG_TOL, cube_errors, degenerate_rays, image_errors, record, worst_element
+from helpers import (ADJ_TOL, CUBE_SIG, CUBE_TOL, IMG_TOL, cube_errors, degenerate_rays, image_errors, record,
+                     rel_dot, worst_element)
 from tomograpy_gb300 import batch, synthetic
 from tomograpy_gb300.infoarray import InfoArray
 
@@ -128,8 +129,15 @@ def test_recon256_full_orbit_against_oracle():
     c = torch.zeros((n, n, n), device=dev)
     yt = torch.from_numpy(np.ascontiguousarray(yy.transpose(2, 0, 1))).to(dev).permute(1, 2, 0)
     tg.siddon.run_device("bpj", yt, c, views, mh, T, obstacle="sun")
+    c = c.cpu().numpy()
+    # adjoint at the benchmark size: <P x, y> = <x, P^T y> (float64 dots of the
+    # float32 GPU results)
+    a = float(np.dot(y.astype(np.float64).ravel(), yy.astype(np.float64).ravel()))
+    b = float(np.dot(x.astype(np.float64).ravel(), c.astype(np.float64).ravel()))
+    record("recon256_full_adjoint", rel=rel_dot(a, b))
+    assert rel_dot(a, b) <= ADJ_TOL, rel_dot(a, b)
     cref = _oracle_bpj(vh, ch, yy, (n, n, n))
-    rel, norm = image_errors(c.cpu().numpy(), cref, sig=CUBE_SIG)
+    rel, norm = image_errors(c, cref, sig=CUBE_SIG)
     record("recon256_full_bpj", rel=rel, norm=norm, views=T)
     assert rel <= CUBE_TOL and norm <= CUBE_TOL, (rel, norm)
 

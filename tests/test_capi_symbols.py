@@ -175,3 +175,19 @@ def test_host_alias_rejects_plain_memory(lib):
     assert lib.tg_host_alias(buf, ctypes.byref(out)) != _lib.TG_OK
     assert out.value is None
     assert lib.tg_host_alias(None, ctypes.byref(out)) == _lib.TG_EINVAL
+
+
+def test_packed_launch_rejects_inconsistent_info(lib):
+    # a plan description with no jobs, or more CTAs than a launch takes, is
+    # refused on the host before any launch
+    from tomograpy_gb300.batch import TgPackedInfo
+    P = ctypes.c_void_p
+    lib.tg_packed_projector.argtypes = [P, P, ctypes.c_int32, ctypes.c_int32, P]
+    lib.tg_packed_projector.restype = ctypes.c_int
+    buf = ctypes.create_string_buffer(4096)
+    info = TgPackedInfo(n_jobs=0, rows_per_warp=4, tiles=10, lane_axis=1)
+    st = lib.tg_packed_projector(ctypes.addressof(buf), ctypes.byref(info), _lib.TG_PJ, 0, None)
+    assert st == _lib.TG_EINVAL and b"jobs" in lib.tg_last_error()
+    info = TgPackedInfo(n_jobs=1, rows_per_warp=4, tiles=1 << 31, lane_axis=1)
+    st = lib.tg_packed_projector(ctypes.addressof(buf), ctypes.byref(info), _lib.TG_PJ, 0, None)
+    assert st == _lib.TG_EUNSUPPORTED and b"too large" in lib.tg_last_error()

@@ -8,7 +8,8 @@ import pytest
 
 import oracle
 import tomograpy_gb300 as tg
-from helpers import (ADJ_TOL, CUBE_SIG, CUBE_TOL, IMG_TOL, degenerate_rays, golden, golden_case, image_errors, rel_dot)
+from helpers import (ADJ_TOL, CUBE_SIG, CUBE_TOL, IMG_TOL, degenerate_rays, golden, golden_case, image_errors, record,
+                     rel_dot)
 from tomograpy_gb300 import synthetic
 from tomograpy_gb300.infoarray import InfoArray
 
@@ -253,7 +254,7 @@ def _geometry(n, T, N, lons, d=215.0, lat=0.0, rol=0.0, crval=(0.0, 0.0), dtype=
     return ch, hdrs
 
 
-def _compare_pj_bpj(ch, vh, x, y, obstacle, shape_img):
+def _compare_pj_bpj(ch, vh, x, y, obstacle, shape_img, name="case"):
     n1, n2, T = shape_img
     degen = degenerate_rays(vh, n1, n2)
     data = InfoArray(shape=shape_img, header=_hdrs(vh), dtype=np.float32)
@@ -262,6 +263,7 @@ def _compare_pj_bpj(ch, vh, x, y, obstacle, shape_img):
     oracle.projector(ref, InfoArray(data=x.astype(np.float32).astype(np.float64), header=dict(ch)),
                      obstacle=obstacle)
     rel, norm = image_errors(data, ref, exclude=degen)
+    record(name + "_pj", rel=rel, norm=norm)
     assert rel <= IMG_TOL and norm <= IMG_TOL, ("pj", rel, norm)
     yy = y.astype(np.float32).copy()
     yy[degen] = 0
@@ -270,6 +272,7 @@ def _compare_pj_bpj(ch, vh, x, y, obstacle, shape_img):
     cref = InfoArray(shape=x.shape, header=dict(ch))
     oracle.backprojector(InfoArray(data=yy.astype(np.float64), header=_hdrs(vh)), cref, obstacle=obstacle)
     rel, norm = image_errors(cube, cref, sig=CUBE_SIG)
+    record(name + "_bpj", rel=rel, norm=norm)
     assert rel <= CUBE_TOL and norm <= CUBE_TOL, ("bpj", rel, norm)
 
 
@@ -278,7 +281,7 @@ def test_plain64_full_size_phantom(obstacle):
     ch, vh = synthetic.make_geometry("plain64")
     x = synthetic.phantom(ch, seed=0)
     y = np.random.default_rng(1).random((128, 128, 60))
-    _compare_pj_bpj(ch, vh, x, y, obstacle, (128, 128, 60))
+    _compare_pj_bpj(ch, vh, x, y, obstacle, (128, 128, 60), name="plain64_%s" % obstacle)
 
 
 @pytest.mark.parametrize("seed", [0, 1, 2])
@@ -299,7 +302,7 @@ def test_random_geometry_random_cube(seed):
     # non-square image: 48 x 40
     for h in vh:
         h["CRPIX2"] = 20.0
-    _compare_pj_bpj(ch, vh, x, y, "sun" if seed % 2 == 0 else None, (48, 40, T))
+    _compare_pj_bpj(ch, vh, x, y, "sun" if seed % 2 == 0 else None, (48, 40, T), name="random%d" % seed)
 
 
 def test_observer_inside_cube_and_small_cube_inside_sun():

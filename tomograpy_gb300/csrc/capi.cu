@@ -419,7 +419,10 @@ tg_status tg_packed_projector(const void *plan, const tg_packed_info *info, int3
   const bool four_d = (mode == TG_PJT || mode == TG_BPJT);
   if (mode < TG_PJ || mode > TG_BPJT || four_d != (info->four_d != 0))
     return fail(TG_EINVAL, "mode does not match the plan (3-D / 4-D)");
+  if (info->n_jobs <= 0) return fail(TG_EINVAL, "plan has %d jobs", info->n_jobs);
   if (info->tiles <= 0) return TG_OK;
+  if (info->tiles > 2147483647LL) return fail(TG_EUNSUPPORTED, "packed launch of %lld CTAs is too large",
+                                              (long long)info->tiles);
   if (info->idx64 && (info->lane_axis != 1 || info->batch_steps != 0))
     return fail(TG_EINVAL, "a plan with 64-bit cube offsets takes the default schedule");
   return launch_status(tg::launch_packed(plan, info->n_jobs, info->tiles, info->rows_per_warp, info->idx64 != 0,

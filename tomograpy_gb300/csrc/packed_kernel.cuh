@@ -65,6 +65,7 @@ __global__ void __launch_bounds__(kThreads, packed_min_blocks(MODE))
   local /= J.gx;
   const int by = (int)(local % J.gy);
   const int t = (int)(local / J.gy);
+  if (t >= J.G.n_views) return;  // a tile count beyond the plan's (whole CTA)
   constexpr bool PJ = (MODE == TG_PJ || MODE == TG_PJT);
   unsigned long long *acc = DET ? reinterpret_cast<unsigned long long *>(ws + J.ws_off + 256) : nullptr;
   const DetScale *dsc = DET ? reinterpret_cast<const DetScale *>(ws + J.ws_off) : nullptr;

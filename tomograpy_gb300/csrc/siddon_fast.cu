@@ -4,19 +4,26 @@
 
 namespace tg {
 
-template <int MODE, typename IDX>
+template <int MODE, typename IDX, int BATCH = 0>
 static void launch_mode(const Geometry &G, bool sun, const float *xin, float *xout, dim3 grid, cudaStream_t s) {
-  if (sun) fast_kernel<MODE, true, IDX, false><<<grid, kThreads, 0, s>>>(G, xin, xout, nullptr, nullptr);
-  else fast_kernel<MODE, false, IDX, false><<<grid, kThreads, 0, s>>>(G, xin, xout, nullptr, nullptr);
+  if (sun) fast_kernel<MODE, true, IDX, false, BATCH><<<grid, kThreads, 0, s>>>(G, xin, xout, nullptr, nullptr);
+  else fast_kernel<MODE, false, IDX, false, BATCH><<<grid, kThreads, 0, s>>>(G, xin, xout, nullptr, nullptr);
+}
+
+// projections over fine cubes take the longer batches
+template <int MODE, typename IDX>
+static void launch_pj(const Geometry &G, bool sun, const float *xin, float *xout, dim3 grid, cudaStream_t s) {
+  if (fine_projection(G)) launch_mode<MODE, IDX, TG_PJ_FINE_BATCH>(G, sun, xin, xout, grid, s);
+  else launch_mode<MODE, IDX>(G, sun, xin, xout, grid, s);
 }
 
 template <typename IDX>
 static void launch_idx(const Geometry &G, int mode, bool sun, float *data, float *map, dim3 grid,
                        cudaStream_t s) {
   switch (mode) {
-  case TG_PJ: launch_mode<TG_PJ, IDX>(G, sun, map, data, grid, s); break;
+  case TG_PJ: launch_pj<TG_PJ, IDX>(G, sun, map, data, grid, s); break;
   case TG_BPJ: launch_mode<TG_BPJ, IDX>(G, sun, data, map, grid, s); break;
-  case TG_PJT: launch_mode<TG_PJT, IDX>(G, sun, map, data, grid, s); break;
+  case TG_PJT: launch_pj<TG_PJT, IDX>(G, sun, map, data, grid, s); break;
   default: launch_mode<TG_BPJT, IDX>(G, sun, data, map, grid, s); break;
   }
 }

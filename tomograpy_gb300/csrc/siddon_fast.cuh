@@ -66,6 +66,19 @@ namespace tg {
 #ifndef TG_PJ_LAG
 #define TG_PJ_LAG 8
 #endif
+// projection over fine cubes (every axis at least TG_PJ_FINE_MIN_N voxels):
+// longer batches.  A batch's running sums drift by ~B ulps of its extent
+// (~B voxel widths), so a pixel's relative error grows like B^2 / n for n
+// voxels along the ray: 32-step batches measured 1.3e-5 per-pixel at 64^3
+// x 128^2 (24-step: 6.5e-6) and 6.7e-6 at 256^3 x 512^2 (24-step: 4.8e-6).
+// They pay off on long rays only: 15.75 -> 15.37 ms at 256^3 x 360 x 512^2,
+// but 5.50 -> 5.58 ms for 128^3 x 28 frames x 784 x 256^2.
+#ifndef TG_PJ_FINE_BATCH
+#define TG_PJ_FINE_BATCH 32
+#endif
+#ifndef TG_PJ_FINE_MIN_N
+#define TG_PJ_FINE_MIN_N 256
+#endif
 #ifndef TG_BPJ_BATCH
 #define TG_BPJ_BATCH 24
 #endif
@@ -789,9 +802,8 @@ __device__ __forceinline__ void trace_fast(const Geometry &G, const tg_image_hea
     // kLag steps after its gather was issued: the gather's latency is hidden
     // behind the walk and only kLag values are live at a time (which is what
     // lets the projection run at 4 CTAs per SM: 16.60 -> 15.75 ms against
-    // summing the whole batch after it; 32-step batches would reach 15.36 ms
-    // but their running sums cost accuracy on coarse cubes -- 1.3e-5
-    // per-pixel at 64^3 x 128^2).  The summation order is unchanged.
+    // summing the whole batch after it at 24 steps, 15.36 ms at the 32 steps
+    // of fine cubes).  The summation order is unchanged.
     constexpr int kLag = TG_PJ_LAG < kBatch - 1 ? TG_PJ_LAG : kBatch - 2;
     float L[kBatch];
     float v[kBatch];
@@ -937,12 +949,19 @@ __device__ __forceinline__ void tile_body(const Geometry &G, int t, int col0, in
 // Modes: 0 = PJ, 1 = BPJ, 2 = PJT, 3 = BPJT, kModeCount; DET: backprojection
 // into the 64-bit fixed-point accumulator `acc64` instead of red.add.f32.
 // Grid (N2 / 32, N1 / kFastRows, views).
-template <int MODE, bool SUN, typename IDX, bool DET>
+// BATCH: steps per drift batch, 0 for the direction's default.
+template <int MODE, bool SUN, typename IDX, bool DET, int BATCH = 0>
 __global__ void __launch_bounds__(kThreads, min_blocks(MODE))
 fast_kernel(const Geometry G, const float *__restrict__ xin, float *__restrict__ xout,
             unsigned long long *__restrict__ acc64, const DetScale *__restrict__ dsc) {
-  tile_body<MODE, SUN, IDX, DET, kFastRowsPerWarp>(G, G.view0 + blockIdx.z, (G.bx0 + blockIdx.x) * 32,
-                                                   (G.by0 + blockIdx.y) * kFastRows, xin, xout, acc64, dsc);
+  tile_body<MODE, SUN, IDX, DET, kFastRowsPerWarp, true, BATCH>(G, G.view0 + blockIdx.z, (G.bx0 + blockIdx.x) * 32,
+                                                                (G.by0 + blockIdx.y) * kFastRows, xin, xout,
+                                                                acc64, dsc);
+}
+
+// Whether a projection over this cube takes the fine-cube batch length.
+inline bool fine_projection(const Geometry &G) {
+  return G.n[0] >= TG_PJ_FINE_MIN_N && G.n[1] >= TG_PJ_FINE_MIN_N && G.n[2] >= TG_PJ_FINE_MIN_N;
 }
 
 }  // namespace tg

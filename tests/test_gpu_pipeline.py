@@ -85,6 +85,34 @@ def test_pinned_host_stack_traced_in_place(layout, use_mask):
     assert _lib.host_alias(torch.empty(4)) is None
 
 
+@pytest.mark.parametrize("layout", ["reference", "view_major"])
+def test_host_buffers_reusable_when_the_call_returns(layout):
+    """Once project / backproject return, the operator no longer reads the
+    caller's pinned host cube or stack (in-place tracing, row-block staging
+    and plain copies alike): overwriting them at once leaves the results
+    equal to the device path's."""
+    ch, vh = synthetic.make_geometry({"n": 40, "T": 9, "N": 112, "d": 215.0, "lon_range": (0.3, 5.0)})
+    op = lo_wrapper.siddon_lo(vh, ch, obstacle="sun", dtype=np.float32)
+    x = torch.from_numpy(synthetic.phantom(ch, seed=4) / np.float32(1e8))
+    y = torch.from_numpy(np.random.default_rng(2).random(op.data_shape).astype(np.float32))
+    ref = op.project(x.cuda()).cpu()
+    cref = op.backproject(y.cuda()).cpu().numpy()
+    xh = x.pin_memory()
+    res = op.project(xh)                      # device result from a pinned host cube
+    xh.fill_(float("nan"))
+    torch.testing.assert_close(res.cpu(), ref, rtol=0, atol=0)
+    if layout == "reference":
+        yh = torch.empty(op.data_shape, dtype=torch.float32).pin_memory()
+    else:
+        yh = torch.empty((9, 112, 112), dtype=torch.float32).pin_memory().permute(1, 2, 0)
+    for out in (None, torch.empty(op.cube_shape, device="cuda")):
+        yh.copy_(y)
+        c = op.backproject(yh, out=out)
+        yh.fill_(float("nan"))
+        rel, norm = image_errors(c.cpu().numpy(), cref, sig=CUBE_SIG)
+        assert rel <= CUBE_TOL and norm <= CUBE_TOL, (layout, out is None, rel, norm)
+
+
 def test_overwrite_projection_through_the_c_abi():
     """TG_OVERWRITE on a device stack: every pixel written, equal to
     zero-then-project; rejected for backprojections."""

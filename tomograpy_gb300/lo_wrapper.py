@@ -82,7 +82,10 @@ class Siddon(LinearOperator):
     # -- device interface ------------------------------------------------
     def _dev(self, a, shape):
         if torch.is_tensor(a):
-            t = a if a.is_cuda else a.to(self.device, non_blocking=True)
+            # a host tensor is copied before the call returns, so its owner may
+            # reuse it at once (an asynchronous copy from pinned memory could
+            # still be reading it)
+            t = a if a.is_cuda else a.to(self.device)
         else:
             t = torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=self.dtype))).to(self.device)
         return t.reshape(shape)
@@ -186,6 +189,7 @@ class Siddon(LinearOperator):
             S.run_device(mode, yd[a:b], x, views, self.mh, self.n_views,
                          None if self.mask is None else self.mask[a:b], self.obstacle)
         yd.record_stream(copy)
+        copy.synchronize()   # every block has left the caller's host stack
         return self._out(x, out)
 
     def project(self, x, out=None):
@@ -236,7 +240,7 @@ class Siddon(LinearOperator):
         else:
             S.run_device("bpjt" if self.four_d else "bpj", yd, x, self.views_dev, self.mh, self.n_views, self.mask,
                          self.obstacle, data_ptr=alias)
-        if alias is not None and out is None:
+        if alias is not None:
             torch.cuda.current_stream().synchronize()   # the caller may reuse its host stack at once
         return self._out(x, out)
 

@@ -22,7 +22,10 @@ EPS23 = F(1.1920929e-7)  # 2^-23
 
 
 def fma(a, b, c):
-    return (np.asarray(a, np.float64) * np.asarray(b, np.float64) + np.asarray(c, np.float64)).astype(F)
+    # 0 * inf (a family parallel to the planes) gives NaN here as on the GPU;
+    # callers select those lanes away
+    with np.errstate(invalid="ignore"):
+        return (np.asarray(a, np.float64) * np.asarray(b, np.float64) + np.asarray(c, np.float64)).astype(F)
 
 
 def make_rays(n_rays, seed, kind):

@@ -32,7 +32,8 @@
 //    start before the stop parameter, so a batch needs no per-step test and
 //    its gathers / atomics are issued together; inside a batch the crossings
 //    advance by running sums (one add) in a frame local to the batch and are
-//    recomputed exactly after it;
+//    recomputed exactly after it (24-step batches; 32 for projections over
+//    cubes of at least 256 voxels per axis);
 //  * the "sun" obstacle: the reference tests |M + ac u|^2 > 1 at every voxel
 //    entry (:575).  Here the walk runs unchecked up to the sphere-entry
 //    parameter minus an error bound; from there on every voxel entry is tested
